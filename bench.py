@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Allen-Cahn phase-field LBM step.
+
+Workload (default): the drop-in GPU case -- 150x150x107 D3Q19 grid, ridge
+substrate (R* = 1, R_d = 22.5, smooth solid fraction), droplet R = 22.5 at
+(75, 75, 80) with impact velocity (0, 0, -0.05), theta_eq = 162 deg,
+alpha_geo = 1.5, rho_l/rho_g = 828, sigma = 0.01424, tau = 0.53, float32.
+Inputs are synthetic, built by the package's generators (same arrays as the
+reference's generators).
+
+One "step" is one lattice time step of the whole grid.  Reported:
+  value      MLUPS (million lattice-node updates per second) over K timed
+             steps with the state resident on the device, CUDA events on the
+             launching stream.  The state (f, g: 732 MB) is larger than L2,
+             so no flush is needed between steps.
+  e2e        the same metric through the public API (AllenCahnSolver) from
+             host numpy arrays: construction, set_solid, init_fields (H2D),
+             K steps, the sweep drivers' read of phi to host every 50 steps
+             (D2H), final spread measurement.
+  roofline   the dominant kernel (k_collide): algorithmic bytes per launch /
+             its CUDA-event duration, against the measured HBM copy peak.
+  cpu_baseline  the numpy oracle (oracle/ac_oracle.py) on a bounded sample of
+             the same workload, one host core.
+
+--impl reference times the CPU implementation of the path (the oracle port;
+the reference itself is Python/PyTorch and is not present on the GPU host)
+on the same workload and prints the same JSON line with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "pytorch-lbm_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+# Algorithmic bytes per node and step, float32 state: f and g (2 x 19
+# populations), u (3) and the previous phi (1), each read once and written
+# once: 2 x 4 x (38 + 3 + 1) = 336 B.
+B_ALG_STEP = 336
+# k_collide reads those 168 B plus this step's phi (4 B) and the node class
+# byte, and writes the 168 B.
+B_ALG_COLLIDE = 341
+# k_phi reads f (76 B) and the class byte and writes phi (4 B).
+B_ALG_PHI = 81
+
+WORKLOADS = {
+    "ridge150": dict(grid=(150, 150, 107), substrate=("ridge", 1.0, 22.5), center=(75, 75, 80),
+                     radius=22.5, u=(0.0, 0.0, -0.05), theta=162.0,
+                     label="ridge 150x150x107 D3Q19 droplet impact, theta=162, alpha_geo=1.5"),
+    "flat64": dict(grid=(64, 64, 48), substrate=("flat_z2",), center=(32, 32, 14), radius=12.0,
+                   u=(0.0, 0.0, 0.0), theta=120.0,
+                   label="flat 64x64x48 D3Q19 static droplet, theta=120, alpha_geo=1.5"),
+}
+
+
+def make_case(name):
+    from geometry.substrate import create_substrate_with_fraction
+    from lbm.fe_config import FEConfig
+    from lbm.fe_droplet import create_fe_droplet_with_impact
+    w = WORKLOADS[name]
+    nx, ny, nz = w["grid"]
+    cfg = FEConfig(nx=nx, ny=ny, nz=nz, rho_l=1.0, rho_g=1.0 / 828.0, sigma=0.01424, xi=4.0,
+                   tau_l=0.53, tau_g=0.53, theta_eq=w["theta"], device="cuda", max_steps=2000)
+    if w["substrate"][0] == "flat_z2":
+        solid = np.zeros((nx, ny, nz), dtype=bool)
+        solid[:, :, :2] = True
+        frac = solid.astype(np.float32)
+    else:
+        t, rs, rd = w["substrate"]
+        solid, frac = create_substrate_with_fraction(nx, ny, nz, t, R_star=rs, R_d=rd)
+    C, _, u = create_fe_droplet_with_impact(nx, ny, nz, center=w["center"], radius=w["radius"], xi=4.0,
+                                            u_impact=w["u"])
+    return cfg, solid, frac, C, u
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel):
+    """DRAM bytes per node of `kernel` from the committed ncu summary
+    (a line 'dram_bytes_per_node <kernel> <value>' in profiles/*.md)."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(pdir, fn)) as fh:
+            for line in fh:
+                parts = line.strip().strip("`").split()
+                if len(parts) == 3 and parts[0] == "dram_bytes_per_node" and parts[1] == kernel:
+                    try:
+                        return float(parts[2])
+                    except ValueError:
+                        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks / throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"lbm_bench_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            with open(self.path) as fh:
+                for line in fh:
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) < 9:
+                        continue
+                    try:
+                        sm.append(float(p[1]))
+                        mx.append(float(p[2]))
+                    except ValueError:
+                        continue
+                    for nm, v in zip(names, p[5:9]):
+                        if v.lower() == "active":
+                            reasons.add(nm)
+            os.remove(self.path)
+        except Exception:
+            return None
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_mlups(name, steps, warmup=1):
+    """The numpy oracle on the same workload: `warmup` + `steps` steps."""
+    from oracle.ac_oracle import OracleSolver
+    cfg, solid, frac, C, u = make_case(name)
+    s = OracleSolver(cfg, dtype=np.float32, geo_amplification=1.5, geometric_wetting=True)
+    s.set_solid(solid, frac)
+    s.init_fields(C, u)
+    for _ in range(warmup):
+        s.step()
+    t = time.perf_counter()
+    for _ in range(steps):
+        s.step()
+    dt = time.perf_counter() - t
+    n = cfg.nx * cfg.ny * cfg.nz
+    return n * steps / dt / 1e6, dt
+
+
+def run_reference_arm(args, rank, world):
+    name = args.workload
+    out = None
+    if rank == 0:
+        # bounded sample: at most 4 timed steps (each ~3-4 s of one core at 2.4 M nodes)
+        steps = max(1, min(args.steps, args.ref_steps))
+        mlups, dt = cpu_oracle_mlups(name, steps, warmup=min(args.warmup, 1))
+        w = WORKLOADS[name]
+        n = int(np.prod(w["grid"]))
+        sample = f"{steps} timed steps (+1 warm-up) of the full {w['grid'][0]}x{w['grid'][1]}x{w['grid'][2]} grid"
+        out = {"impl": "reference", "metric": "MLUPS", "value": mlups, "unit": "MLUPS", "n_gpus": world,
+               "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / steps * 1e3,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic", "config": {"workload": w["label"], "nodes": n, "precision": "fp32"},
+               "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": 1, "kind": "port",
+                                "sample": sample + " with the numpy restatement of the reference step"},
+               "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return out
+
+
+def run_ours(args, rank, world, device):
+    import torch
+    from lbm import _native as nat
+    from lbm.fe_ac_solver import AllenCahnSolver
+    name = args.workload
+    cfg, solid, frac, C, u = make_case(name)
+    cfg.device = str(device)
+    n = cfg.nx * cfg.ny * cfg.nz
+    K, W = args.steps, args.warmup
+
+    # --- device-resident timed region -------------------------------------
+    s = AllenCahnSolver(cfg, dtype=torch.float32, geo_amplification=1.5, geometric_wetting=True)
+    s.set_solid(solid, frac)
+    s.init_fields(C, u)
+    for _ in range(W):
+        s.step()
+    lib, h = s._lib, s._h
+    stream = torch.cuda.current_stream(device)
+    ms3 = (__import__("ctypes").c_float * 3)()
+    barrier(world)
+    torch.cuda.synchronize(device)
+    with Clocks(device.index) as clk:
+        nat.check(lib.lbm_step_profiled(h, K, nat.stream_ptr(stream), ms3), "lbm_step_profiled")
+        torch.cuda.synchronize(device)
+    barrier(world)
+    s.step_count += K
+    phi_ms, col_ms, tot_ms = float(ms3[0]), float(ms3[1]), float(ms3[2])
+    tot_ms = max_over_ranks(tot_ms, world, device)
+    status = s.status()
+    meas = s.measure()
+    if status & nat.STATUS_NAN or meas["has_nan"]:
+        raise RuntimeError("NaN in the benchmark run")
+    value = world * n * K / (tot_ms / 1e3) / 1e6
+
+    # --- end to end through the public API from host arrays ----------------
+    torch.cuda.synchronize(device)
+    barrier(world)
+    t0 = time.perf_counter()
+    s2 = AllenCahnSolver(cfg, dtype=torch.float32, geo_amplification=1.5, geometric_wetting=True)
+    s2.set_solid(solid, frac)
+    s2.init_fields(C, u)
+    reads = 0
+    for k in range(1, K + 1):
+        s2.step()
+        if k % 50 == 0:
+            _ = s2.phi.cpu().numpy()
+            reads += 1
+    m2 = s2.measure()
+    torch.cuda.synchronize(device)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, world, device)
+    e2e = world * n * K / e2e_s / 1e6
+    h2d = solid.nbytes + frac.nbytes + C.nbytes + u.nbytes
+    d2h = reads * n * 4 + 9 * 8
+
+    out = None
+    if rank == 0:
+        peak, peak_kind = peaks()
+        col_s = col_ms / K / 1e3
+        achieved = B_ALG_COLLIDE * n / col_s / 1e9
+        traffic_pn = profiled_traffic("k_collide")
+        step_bw = B_ALG_STEP * n / (tot_ms / K / 1e3) / 1e9
+        w = WORKLOADS[name]
+        cpu = None
+        if not args.no_cpu_baseline:
+            cm, cdt = cpu_oracle_mlups(name, args.cpu_steps, warmup=1)
+            cpu = {"value": cm, "unit": "MLUPS", "cores": 1, "kind": "port",
+                   "sample": f"{args.cpu_steps} steps (+1 warm-up) of the full grid, numpy oracle, "
+                             f"{cdt:.1f} s"}
+        out = {
+            "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": tot_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["label"], "nodes": n, "precision": "fp32 populations, fp32 math, "
+                       "fp64 global sum", "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "state (f, g: 732 MB) larger than L2 (129 MB): no flush"},
+            "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
+                    "d2h_bytes_per_step": d2h / K,
+                    "what": f"AllenCahnSolver from host arrays: create + set_solid + init_fields + {K} steps "
+                            f"+ phi to host every 50 steps + measure; {e2e_s:.3f} s"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic_pn * n if traffic_pn is not None else None,
+                         "kernel": "k_collide", "bytes_per_node": B_ALG_COLLIDE,
+                         "ms_per_launch": col_ms / K},
+            "step_roofline": {"achieved_gbs": step_bw, "bytes_per_node": B_ALG_STEP, "peak": peak,
+                              "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / B_ALG_STEP,
+                              "k_phi_ms": phi_ms / K, "k_collide_ms": col_ms / K},
+            "gpu_launches": 2 * K,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "spread_after": {k2: meas[k2] for k2 in ("Dx", "Dy", "k", "z_com", "volume")},
+        }
+    return out
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ridge150", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--ref-steps", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference_arm(args, rank, world)), flush=True)
+        return
+    import torch
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=device)
+    out = run_ours(args, rank, world, device)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,181 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300 (sm_103a) Allen-Cahn phase-field lattice
+ * Boltzmann time step (D3Q19, conservative Allen-Cahn phase field + Fakhari
+ * pressure-velocity hydrodynamics, geometric-amplification wetting, volume
+ * penalisation, global phi-mass correction).
+ *
+ * One opaque handle owns one grid's device state.  All entry points return 0
+ * on success or a negative LBM_E* code; lbm_last_error() gives a message for
+ * the calling thread.  No exception crosses the ABI.  Pointers are plain host
+ * or device addresses as documented per argument; streams are cudaStream_t
+ * passed as void* (NULL = legacy default stream).
+ *
+ * Each entry point replaces one part of the reference's Python surface
+ * (pytorch-lbm, file:line cited per function).  Layout of every field is the
+ * reference's: C-contiguous (nx, ny, nz), z fastest; vectors (3, nx, ny, nz);
+ * populations (19, nx, ny, nz) in the D3Q19 order of lbm/lattice.py:70-81.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define LBM_OK 0
+#define LBM_E_ARG -1        /* invalid argument / size / null pointer         */
+#define LBM_E_CUDA -2       /* a CUDA runtime call failed                     */
+#define LBM_E_STATE -3      /* call out of order (e.g. step before init)      */
+#define LBM_E_UNSUPPORTED -4
+
+/* Precision of the state and of the collision arithmetic. */
+#define LBM_F32 0           /* float populations, float arithmetic            */
+#define LBM_F64 1           /* double populations, double arithmetic          */
+
+/* Element type of a caller array. */
+#define LBM_DT_NONE 0
+#define LBM_DT_F32 1
+#define LBM_DT_F64 2
+
+/* stab_mode values (lbm/fe_ac_solver.py:433-438). */
+#define LBM_STAB_FAKHARI 0  /* F = F_s + F_p + F_m + F_body                   */
+#define LBM_STAB_LIANG 1    /* F = F_s + F_p + F_body                         */
+#define LBM_STAB_NONE 2     /* F = F_s + F_body                               */
+
+/* Field selection bits for lbm_get_fields. */
+#define LBM_FIELD_PHI 1u
+#define LBM_FIELD_RHO 2u
+#define LBM_FIELD_U 4u
+#define LBM_FIELD_P 8u      /* P = sum(g)                                     */
+#define LBM_FIELD_PRESS 16u /* p = P cs^2 (rho cs^2 right after init)         */
+#define LBM_FIELD_MU 32u
+
+/* Status flag bits (lbm_status). */
+#define LBM_STATUS_NAN 1u        /* sum(phi) was NaN/Inf in some step         */
+#define LBM_STATUS_MASS_LOW 2u   /* sum(phi) <= 1e-6: correction skipped      */
+
+/*
+ * Physical and model parameters.  Field meanings and defaults are those of
+ * FEConfig (lbm/fe_config.py:27-150, already derived: beta, kappa, phi_c) and
+ * of the AllenCahnSolver constructor (lbm/fe_ac_solver.py:54-58).
+ */
+typedef struct LbmParams {
+    double rho_l, rho_g, sigma, xi, beta, kappa, phi_c;
+    double tau_l, tau_g, tau_h;   /* tau_f = tau_h if tau_h > 0 else tau_l    */
+    double theta_eq;              /* degrees; 90 disables wetting             */
+    double g_force[3];
+    double boundary_relax;        /* default 0.3                              */
+    double sharpen_reduce;        /* default 0.8                              */
+    double mu_wall_scale;         /* default 1.0                              */
+    double geo_amplification;     /* scalar alpha_geo; default 1.0            */
+    double ac_scale;              /* default 1.0                              */
+    double ghost_scale;           /* <= 0: automatic (3 if |theta-90|>60 else 2) */
+    int32_t stab_mode;            /* LBM_STAB_*                               */
+    int32_t geometric_wetting;    /* 0/1                                      */
+} LbmParams;
+
+typedef struct LbmHandle LbmHandle;
+
+/* Allocate the device state of one nx*ny*nz grid on the current CUDA device.
+ * Replaces AllenCahnSolver.__init__ (lbm/fe_ac_solver.py:54-191).
+ * Only 3-D grids (nz > 1) are supported. */
+int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz,
+               int precision, LbmHandle** out);
+
+/* Free the handle and its device memory. */
+int lbm_destroy(LbmHandle* h);
+
+/* Solid mask (host, N bytes, nonzero = solid) and optional solid fraction
+ * (host, N elements of fraction_dtype, or NULL with LBM_DT_NONE).  Computes
+ * on the host, bit-exact with the reference: partial-solid nodes and their
+ * penalisation fraction, wetting boundary nodes, wall normals (smooth from the
+ * fraction gradient, else discrete), near-wall distance and weight; uploads
+ * the node-class table.  Replaces AllenCahnSolver.set_solid
+ * (lbm/fe_ac_solver.py:193-237) and ConningtonLeeWetting.__init__ /
+ * _precompute_* (lbm/fe_wetting.py:39-367).  Synchronous. */
+int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction,
+                     int fraction_dtype);
+
+/* Initial phase field phi (N elements) and optional velocity u (3N elements,
+ * NULL = zero), of element type src_dtype, in host memory (on_device = 0) or
+ * device memory (on_device = 1).  Sets f = f_eq(phi, u), g = g_eq(0, u) and
+ * the phi-mass reference.  Replaces AllenCahnSolver.init_fields
+ * (lbm/fe_ac_solver.py:239-261).  Asynchronous on `stream`. */
+int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
+                    int on_device, void* stream);
+
+/* Advance nsteps time steps.  Replaces AllenCahnSolver.step
+ * (lbm/fe_ac_solver.py:380-639).  Asynchronous on `stream`; no host sync. */
+int lbm_step(LbmHandle* h, int nsteps, void* stream);
+
+/* As lbm_step, with CUDA events recorded on `stream` around each of the two
+ * kernels of every step; on return (synchronised) kernel_ms[0] and
+ * kernel_ms[1] hold the summed durations of the phi-recovery and collision
+ * kernels and kernel_ms[2] the whole span.  For measurement; same results as
+ * lbm_step. */
+int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3);
+
+/* Write the fields the reference exposes after the last step (or after
+ * init) into caller device buffers of the handle's precision.  `mask` selects
+ * LBM_FIELD_* bits; unselected pointers may be NULL.  Mirrors the attributes
+ * phi, rho, u, P, p, mu_phi of AllenCahnSolver (lbm/fe_ac_solver.py:97-116,
+ * values as assigned in step()). */
+int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u,
+                   void* P, void* p, void* mu, void* stream);
+
+/* Current populations f, g (19N each, caller device buffers of the handle's
+ * precision) as the reference holds them between steps (AllenCahnSolver.f/.g,
+ * lbm/fe_ac_solver.py:97-98). */
+int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream);
+
+/* Geometry tables as computed by lbm_set_geometry, into host buffers (any may
+ * be NULL): node class byte (N), is_boundary (N), wall_normal (3N float32),
+ * wall_weight (N float32), near_wall mask (N), partial mask (N).  Mirrors
+ * ConningtonLeeWetting.is_boundary / wall_normal / wall_weight /
+ * near_wall_mask (lbm/fe_wetting.py:140,147,305-306) and
+ * AllenCahnSolver._partial_mask (lbm/fe_ac_solver.py:210). */
+int lbm_get_geometry(LbmHandle* h, uint8_t* node_class, uint8_t* is_boundary,
+                     float* wall_normal, float* wall_weight, uint8_t* near_wall,
+                     uint8_t* partial);
+
+/* Host-only form of the geometry precompute of lbm_set_geometry: needs no GPU
+ * and no handle.  Wetting is enabled when theta_eq != 90 and kappa > 0; the
+ * top-surface test uses `precision`.  Outputs as in lbm_get_geometry (any may
+ * be NULL).  Same reference code as lbm_set_geometry
+ * (lbm/fe_ac_solver.py:193-237, lbm/fe_wetting.py:122-311). */
+int lbm_geometry_host(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid, const void* fraction,
+                      int fraction_dtype, double theta_eq, double kappa, int precision,
+                      uint8_t* node_class, uint8_t* is_boundary, float* wall_normal,
+                      float* wall_weight, uint8_t* near_wall, uint8_t* partial);
+
+/* Scalars: phi_mass_init (the reference's phi_mass_init), last step's sum of
+ * phi, last mass-correction factor, number of steps taken. */
+int lbm_get_scalars(LbmHandle* h, double* phi_mass_init, double* last_sum_phi,
+                    double* last_correction, int64_t* step_count);
+
+/* Spread diagnostics of the current phi on the device: out[0] volume = sum of
+ * phi with solid zeroed, out[1] C_max, out[2..4] Dx, Dy, Dz extents of the
+ * phi > 0.5 fluid set, out[5] k = Dx/Dy, out[6] z centre of mass of that set,
+ * out[7] its node count, out[8] 1 if phi has a NaN else 0.  Host output,
+ * synchronises `stream`.  Replaces measure_spread_factor
+ * (lbm/fe_measure.py:11-82) and the every-50-steps extent/z_com/NaN check of
+ * scripts/run_thesis_sweep.py:182-216. */
+int lbm_measure(LbmHandle* h, double* out9, void* stream);
+
+/* Sticky status flags (LBM_STATUS_*) accumulated by the device; synchronises. */
+int lbm_status(LbmHandle* h, uint32_t* flags);
+
+/* Message for the last error on the calling thread ("" if none). */
+const char* lbm_last_error(void);
+
+/* Library version string. */
+const char* lbm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

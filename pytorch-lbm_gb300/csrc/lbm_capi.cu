@@ -1,0 +1,534 @@
+// C ABI of the GB300 Allen-Cahn phase-field LBM (declarations and the
+// reference interface each entry point replaces: include/lbm_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+#include "lbm_common.cuh"
+#include "lbm_geometry.h"
+#include "lbm_tables.h"
+
+namespace lbm {
+template <typename T>
+cudaError_t launch_step(const Consts<T>&, const State<T>&, bool, bool, cudaStream_t, cudaEvent_t);
+template <typename T, typename S>
+cudaError_t launch_init(const Consts<T>&, const State<T>&, const S*, const S*, cudaStream_t);
+template <typename T>
+cudaError_t launch_observe(const Consts<T>&, const State<T>&, bool, unsigned, int, T*, T*, T*, T*, T*, T*,
+                           cudaStream_t);
+template <typename T>
+cudaError_t launch_populations(const Consts<T>&, const State<T>&, bool, T*, T*, cudaStream_t);
+template <typename T>
+cudaError_t launch_measure(int, int, int, const T*, const uint8_t*, double*, int, unsigned*, double*,
+                           cudaStream_t);
+}  // namespace lbm
+
+using namespace lbm;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(LBM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+constexpr int kMeasureBlocks = 1024;
+constexpr int kMeasVals = 11;
+
+struct LbmHandle {
+  LbmParams prm;
+  int prec = LBM_F32;
+  int64_t nx = 0, ny = 0, nz = 0, N = 0;
+  int device = 0;
+  size_t tsize = 4;
+  // device memory
+  void* f[2] = {nullptr, nullptr};
+  void* g[2] = {nullptr, nullptr};
+  void* u = nullptr;
+  void* phi = nullptr;
+  void* phi_prev = nullptr;
+  void* relax = nullptr;
+  void* eps = nullptr;
+  uint8_t* cls = nullptr;
+  float* wn = nullptr;
+  double* partials = nullptr;
+  unsigned* counters = nullptr;  // [0] step/init reductions, [1] measure, [2] status
+  void* cbuf = nullptr;          // 2 x T
+  double* scal = nullptr;        // [0] phi_mass_init [1] last sum [2..10] measure output
+  void* meas_phi = nullptr;      // N x T scratch for lbm_measure
+  // derived
+  bool wetting = false;
+  Consts<float> kf{};
+  Consts<double> kd{};
+  Geometry geo;
+  // sequencing
+  bool geometry_set = false, initialized = false;
+  int cur = 0;            // buffer index holding the current state
+  bool raw = true;        // current state is the reference state itself (after init)
+  bool first = true;      // phi*u of the previous step does not exist yet
+  int c_last = 0;         // cbuf slot of the last step's correction
+  int64_t steps = 0;
+  bool last_raw_in = true;  // mode of the last step's input (for P read-out)
+};
+
+namespace {
+
+template <typename T>
+Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
+  const LbmParams& p = h.prm;
+  Consts<T> k;
+  std::memset(&k, 0, sizeof(k));
+  k.nx = (int)h.nx;
+  k.ny = (int)h.ny;
+  k.nz = (int)h.nz;
+  k.N = (int)h.N;
+  const double cs2 = 1.0 / 3.0;
+  const double tau_f = p.tau_h > 0 ? p.tau_h : p.tau_l;
+  const double ac_coeff = 1.0 - 0.5 / tau_f;
+  for (int q = 0; q < kQ; ++q) {
+    const float wf = q == 0 ? (float)(1.0 / 3.0) : (q <= 6 ? (float)(1.0 / 18.0) : (float)(1.0 / 36.0));
+    k.w[q] = (T)wf;
+    k.wc[q] = (T)wf / (T)cs2;
+    k.w2c[q] = (T)2 * k.wc[q];
+    k.wac[q] = (T)ac_coeff * (T)wf;
+  }
+  k.cs2 = (T)cs2;
+  k.two_cs2 = (T)(2.0 * cs2);
+  k.beta4 = (T)(4.0 * p.beta);
+  k.kappa = (T)p.kappa;
+  k.phi_c = (T)p.phi_c;
+  k.W = (T)p.xi;
+  k.rho_l = (T)p.rho_l;
+  k.rho_g = (T)p.rho_g;
+  k.rho_floor = (T)(0.5 * p.rho_l);
+  k.drho = (T)(p.rho_l - p.rho_g);
+  k.visc = (T)((0.5 - p.tau_g) / p.tau_g);
+  k.omega_f = (T)(1.0 / tau_f);
+  k.tau_l = (T)p.tau_l;
+  k.tl_m = (T)(p.tau_l - 0.5);
+  k.tg_m = (T)(p.tau_g - 0.5);
+  k.tau_const = p.tau_g == p.tau_l;
+  k.has_gforce = 0;
+  for (int d = 0; d < 3; ++d) {
+    k.gforce[d] = (T)p.g_force[d];
+    if (p.g_force[d] != 0.0) k.has_gforce = 1;
+  }
+  k.stab_mode = p.stab_mode;
+  k.ac_scale = (T)p.ac_scale;
+  k.sharpen_reduce = (T)p.sharpen_reduce;
+  k.wetting = h.wetting ? 1 : 0;
+  const double deg2rad = M_PI / 180.0;
+  const double th = p.theta_eq * deg2rad;
+  k.linear = (p.theta_eq > 130.0 || p.theta_eq < 50.0) ? 1 : 0;
+  if (k.wetting) {
+    if (k.linear) {
+      const double hh = p.sigma * std::cos(th);
+      double gs = p.ghost_scale;
+      if (!(gs > 0.0)) gs = std::fabs(p.theta_eq - 90.0) > 60.0 ? 3.0 : 2.0;
+      k.h_over_kappa_f = (float)(hh / p.kappa * gs);
+      k.mu_wall_add = (T)((-hh * 2.0) * p.mu_wall_scale);
+    } else {
+      k.pcok_f = (float)(p.phi_c / p.kappa);
+    }
+  }
+  const double cos_t = std::cos(th), sin_t = std::sin(th);
+  k.cos_t = (T)cos_t;
+  k.sin_t = (T)sin_t;
+  k.geometric = (k.wetting && p.geometric_wetting && std::fabs(sin_t) >= 1e-10) ? 1 : 0;
+  k.amp_active = p.geo_amplification > 1.0 ? 1 : 0;
+  k.amp = (T)p.geo_amplification;
+  // boundary-phi relaxation target (fe_ac_solver.py:165-177, 613-616)
+  k.relax_on = 0;
+  if (k.wetting && p.boundary_relax > 0 && p.theta_eq != 90.0) {
+    const double c = std::cos(th);
+    const double disc = 1.0 - 4.0 * (-c / 3.0);
+    double target;
+    if (disc >= 0) target = 0.5 * (1.0 - std::sqrt(disc));
+    else target = 0.5 * (1.0 - std::cos(M_PI - th));
+    if (std::fabs(target - 0.5) > 0.05) {
+      k.relax_on = 1;
+      k.relax_target = (T)target;
+      k.relax_r = (T)p.boundary_relax;
+    }
+  }
+  for (int i = 0; i < 16; ++i) k.ww[i] = (T)ww_lut[i];
+  return k;
+}
+
+template <typename T>
+State<T> make_state(const LbmHandle& h, int in_buf) {
+  State<T> s;
+  std::memset(&s, 0, sizeof(s));
+  s.fin = static_cast<const T*>(h.f[in_buf]);
+  s.gin = static_cast<const T*>(h.g[in_buf]);
+  s.fout = static_cast<T*>(h.f[in_buf ^ 1]);
+  s.gout = static_cast<T*>(h.g[in_buf ^ 1]);
+  s.u = static_cast<T*>(h.u);
+  s.phi_prev = static_cast<T*>(h.phi_prev);
+  s.phi = static_cast<T*>(h.phi);
+  s.relax = static_cast<T*>(h.relax);
+  s.cls = h.cls;
+  s.wn = h.wn;
+  s.eps = static_cast<const T*>(h.eps);
+  s.partials = h.partials;
+  s.counter = h.counters;
+  s.cbuf = static_cast<T*>(h.cbuf);
+  s.scal = h.scal;
+  s.status = h.counters + 2;
+  return s;
+}
+
+void free_all(LbmHandle* h) {
+  void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u, h->phi, h->phi_prev, h->relax, h->eps,
+                  h->cls, h->wn, h->partials, h->counters, h->cbuf, h->scal, h->meas_phi};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+template <typename T>
+const Consts<T>& consts_of(const LbmHandle& h);
+template <>
+const Consts<float>& consts_of<float>(const LbmHandle& h) { return h.kf; }
+template <>
+const Consts<double>& consts_of<double>(const LbmHandle& h) { return h.kd; }
+
+template <typename T>
+int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+  const Consts<T>& k = consts_of<T>(*h);
+  for (int i = 0; i < nsteps; ++i) {
+    State<T> s = make_state<T>(*h, h->cur);
+    s.c_prev = h->c_last;
+    s.c_cur = h->c_last ^ 1;
+    if (ev) CUDA_TRY(cudaEventRecord(ev[2 * i], st));
+    CUDA_TRY(launch_step<T>(k, s, h->raw, h->first, st, ev ? ev[2 * i + 1] : nullptr));
+    h->last_raw_in = h->raw;
+    h->cur ^= 1;
+    h->c_last ^= 1;
+    h->raw = false;
+    h->first = false;
+    ++h->steps;
+  }
+  if (ev) CUDA_TRY(cudaEventRecord(ev[2 * nsteps], st));
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm_last_error(void) { return g_err.c_str(); }
+
+const char* lbm_version(void) { return "lbm_gb300 0.1 (sm_103a)"; }
+
+int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int precision, LbmHandle** out) {
+  if (!params || !out) return fail(LBM_E_ARG, "lbm_create: null argument");
+  *out = nullptr;
+  if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_create: 3-D grids with every extent >= 2 only");
+  if (precision != LBM_F32 && precision != LBM_F64) return fail(LBM_E_ARG, "lbm_create: precision must be LBM_F32 or LBM_F64");
+  const int64_t N = nx * ny * nz;
+  if (N > (int64_t)0x7fffffff / 2) return fail(LBM_E_ARG, "lbm_create: grid too large (N must be < 2^30)");
+  if (params->stab_mode < 0 || params->stab_mode > 2) return fail(LBM_E_ARG, "lbm_create: bad stab_mode");
+  if (!(params->tau_g > 0.5) || !(params->tau_l > 0.5)) return fail(LBM_E_ARG, "lbm_create: tau_l, tau_g must exceed 0.5");
+  if (!(params->xi > 0)) return fail(LBM_E_ARG, "lbm_create: xi must be positive");
+  LbmHandle* h = new (std::nothrow) LbmHandle();
+  if (!h) return fail(LBM_E_ARG, "lbm_create: out of host memory");
+  h->prm = *params;
+  h->prec = precision;
+  h->nx = nx;
+  h->ny = ny;
+  h->nz = nz;
+  h->N = N;
+  h->tsize = precision == LBM_F32 ? 4 : 8;
+  h->wetting = params->theta_eq != 90.0 && params->kappa > 0;
+  cudaGetDevice(&h->device);
+  const size_t T = h->tsize;
+  const int nblocks = (int)((N + kBlock - 1) / kBlock);
+  const size_t npart = std::max<size_t>((size_t)nblocks, (size_t)kMeasureBlocks * kMeasVals);
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  for (int b = 0; b < 2; ++b) {
+    A(&h->f[b], (size_t)Q * N * T);
+    A(&h->g[b], (size_t)Q * N * T);
+  }
+  A(&h->u, 3 * N * T);
+  A(&h->phi, N * T);
+  A(&h->phi_prev, N * T);
+  A(&h->relax, N * T);
+  A(&h->eps, N * T);
+  A((void**)&h->cls, N);
+  A((void**)&h->wn, 3 * N * sizeof(float));
+  A((void**)&h->partials, npart * sizeof(double));
+  A((void**)&h->counters, 4 * sizeof(unsigned));
+  A(&h->cbuf, 2 * T);
+  A((void**)&h->scal, 16 * sizeof(double));
+  A(&h->meas_phi, N * T);
+  if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(h->scal, 0, 16 * sizeof(double));
+  if (e != cudaSuccess) {
+    free_all(h);
+    delete h;
+    return fail(LBM_E_CUDA, std::string("lbm_create: ") + cudaGetErrorString(e));
+  }
+  *out = h;
+  return LBM_OK;
+}
+
+int lbm_destroy(LbmHandle* h) {
+  if (!h) return LBM_OK;
+  free_all(h);
+  delete h;
+  return LBM_OK;
+}
+
+int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, int fraction_dtype) {
+  if (!h || !solid) return fail(LBM_E_ARG, "lbm_set_geometry: null argument");
+  if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
+    return fail(LBM_E_ARG, "lbm_set_geometry: fraction and fraction_dtype disagree");
+  compute_geometry(h->nx, h->ny, h->nz, solid, fraction, fraction_dtype, h->wetting, h->prec == LBM_F64, h->geo);
+  const int64_t N = h->N;
+  CUDA_TRY(cudaMemcpy(h->cls, h->geo.cls.data(), N, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->wn, h->geo.wall_normal.data(), 3 * N * sizeof(float), cudaMemcpyHostToDevice));
+  if (h->prec == LBM_F32) {
+    std::vector<float> eps(N, 0.0f);
+    if (!h->geo.fraction.empty())
+      for (int64_t n = 0; n < N; ++n) eps[n] = (float)h->geo.fraction[n];
+    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * sizeof(float), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<double> eps(N, 0.0);
+    if (!h->geo.fraction.empty()) eps = h->geo.fraction;
+    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  float lut[kWwCodes];
+  near_wall_weights(lut);
+  h->kf = make_consts<float>(*h, lut);
+  h->kd = make_consts<double>(*h, lut);
+  h->geometry_set = true;
+  return LBM_OK;
+}
+
+int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype, int on_device, void* stream) {
+  if (!h || !phi) return fail(LBM_E_ARG, "lbm_init_fields: null argument");
+  if (!h->geometry_set) return fail(LBM_E_STATE, "lbm_init_fields: call lbm_set_geometry first");
+  if (src_dtype != LBM_DT_F32 && src_dtype != LBM_DT_F64) return fail(LBM_E_ARG, "lbm_init_fields: bad src_dtype");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t es = src_dtype == LBM_DT_F32 ? 4 : 8;
+  const int64_t N = h->N;
+  // Host inputs are staged through the (not yet used) second g buffer:
+  // 19 N T-elements hold the 4 N source elements.
+  int in = h->cur;
+  const void* dphi = phi;
+  const void* du = u;
+  if (!on_device) {
+    char* stage = static_cast<char*>(h->g[in ^ 1]);
+    CUDA_TRY(cudaMemcpyAsync(stage, phi, N * es, cudaMemcpyHostToDevice, st));
+    dphi = stage;
+    if (u) {
+      CUDA_TRY(cudaMemcpyAsync(stage + N * es, u, 3 * N * es, cudaMemcpyHostToDevice, st));
+      du = stage + N * es;
+    }
+  }
+  cudaError_t e;
+  if (h->prec == LBM_F32) {
+    State<float> s = make_state<float>(*h, in);
+    e = src_dtype == LBM_DT_F32
+            ? launch_init<float, float>(h->kf, s, (const float*)dphi, (const float*)du, st)
+            : launch_init<float, double>(h->kf, s, (const double*)dphi, (const double*)du, st);
+  } else {
+    State<double> s = make_state<double>(*h, in);
+    e = src_dtype == LBM_DT_F32
+            ? launch_init<double, float>(h->kd, s, (const float*)dphi, (const float*)du, st)
+            : launch_init<double, double>(h->kd, s, (const double*)dphi, (const double*)du, st);
+  }
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_init_fields: ") + cudaGetErrorString(e));
+  h->initialized = true;
+  h->raw = true;
+  h->first = true;
+  h->c_last = 0;
+  h->steps = 0;
+  h->last_raw_in = true;
+  return LBM_OK;
+}
+
+int lbm_step(LbmHandle* h, int nsteps, void* stream) {
+  if (!h) return fail(LBM_E_ARG, "lbm_step: null handle");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_step: call lbm_init_fields first");
+  if (nsteps < 0) return fail(LBM_E_ARG, "lbm_step: negative step count");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return h->prec == LBM_F32 ? do_step<float>(h, nsteps, st) : do_step<double>(h, nsteps, st);
+}
+
+int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3) {
+  if (!h || !kernel_ms3) return fail(LBM_E_ARG, "lbm_step_profiled: null argument");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_step_profiled: call lbm_init_fields first");
+  if (nsteps <= 0) return fail(LBM_E_ARG, "lbm_step_profiled: nsteps must be positive");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  std::vector<cudaEvent_t> ev(2 * (size_t)nsteps + 1, nullptr);
+  for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+  int rc = h->prec == LBM_F32 ? do_step<float>(h, nsteps, st, ev.data()) : do_step<double>(h, nsteps, st, ev.data());
+  float a = 0.f, b = 0.f, tot = 0.f;
+  if (rc == LBM_OK) {
+    cudaError_t e = cudaEventSynchronize(ev.back());
+    for (int i = 0; i < nsteps && e == cudaSuccess; ++i) {
+      float x = 0.f, y = 0.f;
+      e = cudaEventElapsedTime(&x, ev[2 * i], ev[2 * i + 1]);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&y, ev[2 * i + 1], ev[2 * i + 2]);
+      a += x;
+      b += y;
+    }
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&tot, ev.front(), ev.back());
+    if (e != cudaSuccess) rc = fail(LBM_E_CUDA, std::string("lbm_step_profiled: ") + cudaGetErrorString(e));
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  kernel_ms3[0] = a;
+  kernel_ms3[1] = b;
+  kernel_ms3[2] = tot;
+  return rc;
+}
+
+int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u, void* P, void* p, void* mu,
+                   void* stream) {
+  if (!h) return fail(LBM_E_ARG, "lbm_get_fields: null handle");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_get_fields: not initialised");
+  if (((mask & LBM_FIELD_PHI) && !phi) || ((mask & LBM_FIELD_RHO) && !rho) || ((mask & LBM_FIELD_U) && !u) ||
+      ((mask & LBM_FIELD_P) && !P) || ((mask & LBM_FIELD_PRESS) && !p) || ((mask & LBM_FIELD_MU) && !mu))
+    return fail(LBM_E_ARG, "lbm_get_fields: selected output is null");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int mode = h->steps == 0 ? 0 : 1;
+  const int in_buf = h->steps == 0 ? h->cur : (h->cur ^ 1);  // the last step's input buffer
+  cudaError_t e;
+  if (h->prec == LBM_F32) {
+    State<float> s = make_state<float>(*h, in_buf);
+    s.c_cur = h->c_last;
+    e = launch_observe<float>(h->kf, s, h->last_raw_in, mask, mode, (float*)phi, (float*)rho, (float*)u,
+                              (float*)P, (float*)p, (float*)mu, st);
+  } else {
+    State<double> s = make_state<double>(*h, in_buf);
+    s.c_cur = h->c_last;
+    e = launch_observe<double>(h->kd, s, h->last_raw_in, mask, mode, (double*)phi, (double*)rho, (double*)u,
+                               (double*)P, (double*)p, (double*)mu, st);
+  }
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_get_fields: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream) {
+  if (!h) return fail(LBM_E_ARG, "lbm_get_populations: null handle");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_get_populations: not initialised");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (h->prec == LBM_F32) {
+    State<float> s = make_state<float>(*h, h->cur);
+    s.c_cur = h->c_last;
+    e = launch_populations<float>(h->kf, s, h->raw, (float*)f, (float*)g, st);
+  } else {
+    State<double> s = make_state<double>(*h, h->cur);
+    s.c_cur = h->c_last;
+    e = launch_populations<double>(h->kd, s, h->raw, (double*)f, (double*)g, st);
+  }
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_get_populations: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+int lbm_get_geometry(LbmHandle* h, uint8_t* node_class, uint8_t* is_boundary, float* wall_normal,
+                     float* wall_weight, uint8_t* near_wall, uint8_t* partial) {
+  if (!h) return fail(LBM_E_ARG, "lbm_get_geometry: null handle");
+  if (!h->geometry_set) return fail(LBM_E_STATE, "lbm_get_geometry: no geometry");
+  const size_t N = (size_t)h->N;
+  if (node_class) std::memcpy(node_class, h->geo.cls.data(), N);
+  if (is_boundary) std::memcpy(is_boundary, h->geo.boundary.data(), N);
+  if (wall_normal) std::memcpy(wall_normal, h->geo.wall_normal.data(), 3 * N * sizeof(float));
+  if (wall_weight) std::memcpy(wall_weight, h->geo.wall_weight.data(), N * sizeof(float));
+  if (near_wall) std::memcpy(near_wall, h->geo.near_wall.data(), N);
+  if (partial) std::memcpy(partial, h->geo.partial.data(), N);
+  return LBM_OK;
+}
+
+int lbm_geometry_host(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid, const void* fraction,
+                      int fraction_dtype, double theta_eq, double kappa, int precision, uint8_t* node_class,
+                      uint8_t* is_boundary, float* wall_normal, float* wall_weight, uint8_t* near_wall,
+                      uint8_t* partial) {
+  if (!solid) return fail(LBM_E_ARG, "lbm_geometry_host: null solid");
+  if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_geometry_host: 3-D grids only");
+  if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
+    return fail(LBM_E_ARG, "lbm_geometry_host: fraction and fraction_dtype disagree");
+  Geometry g;
+  compute_geometry(nx, ny, nz, solid, fraction, fraction_dtype, theta_eq != 90.0 && kappa > 0,
+                   precision == LBM_F64, g);
+  const size_t N = (size_t)(nx * ny * nz);
+  if (node_class) std::memcpy(node_class, g.cls.data(), N);
+  if (is_boundary) std::memcpy(is_boundary, g.boundary.data(), N);
+  if (wall_normal) std::memcpy(wall_normal, g.wall_normal.data(), 3 * N * sizeof(float));
+  if (wall_weight) std::memcpy(wall_weight, g.wall_weight.data(), N * sizeof(float));
+  if (near_wall) std::memcpy(near_wall, g.near_wall.data(), N);
+  if (partial) std::memcpy(partial, g.partial.data(), N);
+  return LBM_OK;
+}
+
+int lbm_get_scalars(LbmHandle* h, double* phi_mass_init, double* last_sum_phi, double* last_correction,
+                    int64_t* step_count) {
+  if (!h) return fail(LBM_E_ARG, "lbm_get_scalars: null handle");
+  double sc[2] = {0.0, 0.0};
+  if (h->initialized) CUDA_TRY(cudaMemcpy(sc, h->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+  if (phi_mass_init) *phi_mass_init = sc[0];
+  if (last_sum_phi) *last_sum_phi = sc[1];
+  if (last_correction) {
+    double c = 1.0;
+    if (h->initialized && h->steps > 0) {
+      if (h->prec == LBM_F32) {
+        float v;
+        CUDA_TRY(cudaMemcpy(&v, static_cast<float*>(h->cbuf) + h->c_last, sizeof(float), cudaMemcpyDeviceToHost));
+        c = v;
+      } else {
+        CUDA_TRY(cudaMemcpy(&c, static_cast<double*>(h->cbuf) + h->c_last, sizeof(double), cudaMemcpyDeviceToHost));
+      }
+    }
+    *last_correction = c;
+  }
+  if (step_count) *step_count = h->steps;
+  return LBM_OK;
+}
+
+int lbm_measure(LbmHandle* h, double* out9, void* stream) {
+  if (!h || !out9) return fail(LBM_E_ARG, "lbm_measure: null argument");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_measure: not initialised");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = lbm_get_fields(h, LBM_FIELD_PHI, h->meas_phi, nullptr, nullptr, nullptr, nullptr, nullptr, stream);
+  if (rc) return rc;
+  cudaError_t e;
+  if (h->prec == LBM_F32)
+    e = launch_measure<float>((int)h->nx, (int)h->ny, (int)h->nz, (const float*)h->meas_phi, h->cls, h->partials,
+                              kMeasureBlocks, h->counters + 1, h->scal + 2, st);
+  else
+    e = launch_measure<double>((int)h->nx, (int)h->ny, (int)h->nz, (const double*)h->meas_phi, h->cls, h->partials,
+                               kMeasureBlocks, h->counters + 1, h->scal + 2, st);
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_measure: ") + cudaGetErrorString(e));
+  CUDA_TRY(cudaMemcpyAsync(out9, h->scal + 2, 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return LBM_OK;
+}
+
+int lbm_status(LbmHandle* h, uint32_t* flags) {
+  if (!h || !flags) return fail(LBM_E_ARG, "lbm_status: null argument");
+  unsigned v = 0;
+  CUDA_TRY(cudaMemcpy(&v, h->counters + 2, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  *flags = v;
+  return LBM_OK;
+}
+
+}  // extern "C"

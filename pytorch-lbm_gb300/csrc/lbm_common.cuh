@@ -1,0 +1,128 @@
+// Shared definitions of the GB300 Allen-Cahn LBM kernels: D3Q19 tables, node
+// classes, per-step constants and device-state pointers.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace lbm {
+
+constexpr int Q = 19;
+constexpr int kBlock = 256;  // threads per block of every node-parallel kernel
+
+// D3Q19 velocity set in the population order of the reference
+// (pytorch-lbm lbm/lattice.py:70-95).  Written as constexpr functions so that
+// fully unrolled loops fold every component to an immediate.
+__host__ __device__ constexpr int ex(int q) {
+  return (q == 1 || q == 7 || q == 10 || q == 11 || q == 14) ? 1
+       : (q == 2 || q == 8 || q == 9 || q == 12 || q == 13) ? -1 : 0;
+}
+__host__ __device__ constexpr int ey(int q) {
+  return (q == 3 || q == 7 || q == 8 || q == 15 || q == 18) ? 1
+       : (q == 4 || q == 9 || q == 10 || q == 16 || q == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int ez(int q) {
+  return (q == 5 || q == 11 || q == 12 || q == 15 || q == 16) ? 1
+       : (q == 6 || q == 13 || q == 14 || q == 17 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int opp(int q) {
+  return q == 0 ? 0 : (q <= 6 ? ((q & 1) ? q + 1 : q - 1)
+                              : (q <= 10 ? (q <= 8 ? q + 2 : q - 2)
+                                         : (q <= 14 ? (q <= 12 ? q + 2 : q - 2)
+                                                    : (q <= 16 ? q + 2 : q - 2))));
+}
+__host__ __device__ constexpr int ecomp(int q, int d) { return d == 0 ? ex(q) : (d == 1 ? ey(q) : ez(q)); }
+
+// Node class byte.
+constexpr uint8_t kSolid = 1;     // solid node (bounce-back)
+constexpr uint8_t kBoundary = 2;  // fluid node with a solid D3Q19 neighbour (wetting)
+constexpr uint8_t kPartial = 4;   // volume-penalised partial-solid node
+constexpr uint8_t kTop = 8;       // boundary node with |n_z|/|n| > 0.5 (boundary-phi relaxation)
+constexpr int kWwShift = 4;       // bits 4..7: near-wall weight code (0..11 distance, 12 far, 13 solid)
+constexpr int kWwFar = 12;
+constexpr int kWwSolid = 13;
+
+// Periodic neighbour offsets of one node: o?[d + 1] is the flat-index offset
+// of a step d in {-1, 0, +1} along that axis, wrapped at the domain edge.
+struct Nbr {
+  int ox[3], oy[3], oz[3];
+  __device__ __forceinline__ int at(int n, int dx, int dy, int dz) const {
+    return n + ox[dx + 1] + oy[dy + 1] + oz[dz + 1];
+  }
+};
+
+__device__ __forceinline__ Nbr make_nbr(int n, int nx, int ny, int nz, int* ix_out, int* iy_out,
+                                        int* iz_out) {
+  const int iz = n % nz;
+  const int t = n / nz;
+  const int iy = t % ny;
+  const int ix = t / ny;
+  const int sx = ny * nz, sy = nz;
+  Nbr b;
+  b.ox[0] = ix == 0 ? (nx - 1) * sx : -sx;
+  b.ox[1] = 0;
+  b.ox[2] = ix == nx - 1 ? -(nx - 1) * sx : sx;
+  b.oy[0] = iy == 0 ? (ny - 1) * sy : -sy;
+  b.oy[1] = 0;
+  b.oy[2] = iy == ny - 1 ? -(ny - 1) * sy : sy;
+  b.oz[0] = iz == 0 ? nz - 1 : -1;
+  b.oz[1] = 0;
+  b.oz[2] = iz == nz - 1 ? -(nz - 1) : 1;
+  *ix_out = ix;
+  *iy_out = iy;
+  *iz_out = iz;
+  return b;
+}
+
+// Constants of one grid's time step in the compute type T.  Every value is
+// the reference's python-double expression rounded once to T at the point the
+// reference mixes it into a T tensor.
+template <typename T>
+struct Consts {
+  int nx, ny, nz, N;
+  T w[Q];      // lattice weights (float32 table, widened)
+  T wc[Q];     // w_i / cs2                      (stencil weights)
+  T w2c[Q];    // 2 w_i / cs2                    (laplacian weights)
+  T wac[Q];    // (1 - 1/(2 tau_f)) w_i          (Allen-Cahn source)
+  T cs2, two_cs2;
+  T beta4, kappa, phi_c, W;
+  T rho_l, rho_g, rho_floor, drho;
+  T visc;      // (1/2 - tau_g) / tau_g
+  T omega_f;   // 1 / tau_f
+  T tau_l, tl_m, tg_m;  // tau_l, tau_l - 1/2, tau_g - 1/2
+  int tau_const;        // tau_l == tau_g
+  T gforce[3];
+  int has_gforce;
+  int stab_mode;
+  T ac_scale, sharpen_reduce;
+  int wetting, linear, geometric, amp_active, relax_on;
+  float h_over_kappa_f;  // ghost offset factor (linear), float32 like n.e_i
+  float pcok_f;          // phi_c / kappa (quadratic), float32 like n.e_i
+  T mu_wall_add;         // mu_wall * mu_wall_scale (linear)
+  T cos_t, sin_t, amp;
+  T relax_r, relax_target;
+  T ww[16];              // near-wall weight by code (float32 values)
+};
+
+// Device state of one grid.
+template <typename T>
+struct State {
+  const T* fin;   // populations read this step (post-collision of the last step, or raw)
+  const T* gin;
+  T* fout;        // post-collision populations written this step
+  T* gout;
+  T* u;           // velocity [3][N], in place
+  T* phi_prev;    // phi of the last step (phi*u of the last step = phi_prev*u)
+  T* phi;         // phi of this step (written by the phi kernel)
+  T* relax;       // boundary-phi relaxation: pending phi target / scale, -1 = none
+  const uint8_t* cls;
+  const float* wn;  // wall normal [3][N] (non-zero at boundary nodes only)
+  const T* eps;     // solid fraction (read at partial nodes only)
+  double* partials; // one per block
+  unsigned* counter;
+  T* cbuf;          // mass-correction factor of the last two steps
+  double* scal;     // [0] phi_mass_init, [1] last sum(phi)
+  unsigned* status;
+  int c_prev, c_cur;  // cbuf slots: factor applied to fin, factor produced this step
+};
+
+}  // namespace lbm

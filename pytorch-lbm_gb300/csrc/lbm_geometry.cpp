@@ -1,0 +1,235 @@
+// Host-side geometry precompute of one grid: partial-solid nodes, wetting
+// boundary nodes, wall normals, near-wall distance / weight and the node-class
+// byte read by the kernels.
+//
+// Bit-exact with the reference's set_solid + ConningtonLeeWetting precompute
+// (pytorch-lbm lbm/fe_ac_solver.py:193-237, lbm/fe_wetting.py:122-311).  Must
+// be compiled with floating-point contraction off: the smooth normals repeat
+// numpy's float32/float64 operation sequence exactly.
+#include "lbm_geometry.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lbm_tables.h"
+
+namespace lbm {
+
+namespace {
+
+inline int64_t idx(int64_t ix, int64_t iy, int64_t iz, int64_t ny, int64_t nz) {
+  return (ix * ny + iy) * nz + iz;
+}
+
+inline int64_t wrap(int64_t i, int64_t n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// Smooth wall normals -grad(frac)/|grad(frac)| at boundary nodes, with
+// np.gradient's stencil (central inside, one-sided first order at the edges)
+// evaluated in the fraction's own type F (fe_wetting.py:242-267).
+template <typename F>
+void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, int64_t ny, int64_t nz,
+                    std::vector<float>& wn) {
+  const int64_t N = nx * ny * nz;
+  auto grad_axis = [&](int64_t ix, int64_t iy, int64_t iz, int axis) -> F {
+    int64_t n_ax = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    int64_t i = axis == 0 ? ix : (axis == 1 ? iy : iz);
+    auto at = [&](int64_t j) -> F {
+      return axis == 0 ? frac[idx(j, iy, iz, ny, nz)]
+           : (axis == 1 ? frac[idx(ix, j, iz, ny, nz)] : frac[idx(ix, iy, j, ny, nz)]);
+    };
+    if (i == 0) return (F)(at(1) - at(0)) / (F)1.0;
+    if (i == n_ax - 1) return (F)(at(n_ax - 1) - at(n_ax - 2)) / (F)1.0;
+    return (F)(at(i + 1) - at(i - 1)) / (F)2.0;
+  };
+  for (int64_t ix = 0; ix < nx; ++ix)
+    for (int64_t iy = 0; iy < ny; ++iy)
+      for (int64_t iz = 0; iz < nz; ++iz) {
+        const int64_t n = idx(ix, iy, iz, ny, nz);
+        if (!bnd[n]) continue;
+        const F g0 = grad_axis(ix, iy, iz, 0);
+        const F g1 = grad_axis(ix, iy, iz, 1);
+        const F g2 = grad_axis(ix, iy, iz, 2);
+        F acc = (F)0;
+        acc = acc + g0 * g0;
+        acc = acc + g1 * g1;
+        acc = acc + g2 * g2;
+        F mag = std::sqrt(acc);
+        if (mag < (F)1e-10) mag = (F)1e-10;
+        wn[n] = (float)((-g0) / mag);
+        wn[N + n] = (float)((-g1) / mag);
+        wn[2 * N + n] = (float)((-g2) / mag);
+      }
+}
+
+}  // namespace
+
+int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in, const void* fraction,
+                     int fraction_dtype, bool wetting, bool dbl_precision, Geometry& g) {
+  const int64_t N = nx * ny * nz;
+  g.solid.assign(N, 0);
+  for (int64_t n = 0; n < N; ++n) g.solid[n] = solid_in[n] ? 1 : 0;
+  g.partial.assign(N, 0);
+  g.fraction.assign(0, 0.0);
+  if (fraction_dtype != 0) {
+    g.fraction.resize(N);
+    for (int64_t n = 0; n < N; ++n) {
+      bool part;
+      if (fraction_dtype == 1) {
+        const float v = static_cast<const float*>(fraction)[n];
+        g.fraction[n] = (double)v;
+        part = v > 0.01f && v < 0.99f;
+      } else {
+        const double v = static_cast<const double*>(fraction)[n];
+        g.fraction[n] = v;
+        part = v > 0.01 && v < 0.99;
+      }
+      g.partial[n] = (part && !g.solid[n]) ? 1 : 0;
+    }
+  }
+  g.boundary.assign(N, 0);
+  g.near_wall.assign(N, 0);
+  g.top.assign(N, 0);
+  g.wall_normal.assign(3 * N, 0.0f);
+  g.wall_weight.assign(N, 0.0f);
+  g.dist.assign(N, 100);
+  g.n_boundary = 0;
+
+  if (wetting) {
+    // boundary: fluid node whose periodic neighbour x - e_q is solid for some q
+    for (int64_t ix = 0; ix < nx; ++ix)
+      for (int64_t iy = 0; iy < ny; ++iy)
+        for (int64_t iz = 0; iz < nz; ++iz) {
+          const int64_t n = idx(ix, iy, iz, ny, nz);
+          if (g.solid[n]) continue;
+          for (int q = 1; q < kQ; ++q) {
+            const int64_t m = idx(wrap(ix - kE[q][0], nx), wrap(iy - kE[q][1], ny), wrap(iz - kE[q][2], nz), ny, nz);
+            if (g.solid[m]) {
+              g.boundary[n] = 1;
+              ++g.n_boundary;
+              break;
+            }
+          }
+        }
+    // wall normals
+    if (fraction_dtype == 1) {
+      smooth_normals(static_cast<const float*>(fraction), g.boundary, nx, ny, nz, g.wall_normal);
+    } else if (fraction_dtype == 2) {
+      smooth_normals(static_cast<const double*>(fraction), g.boundary, nx, ny, nz, g.wall_normal);
+    } else {
+      // discrete neighbour counting with non-periodic bounds (fe_wetting.py:152-178)
+      for (int64_t ix = 0; ix < nx; ++ix)
+        for (int64_t iy = 0; iy < ny; ++iy)
+          for (int64_t iz = 0; iz < nz; ++iz) {
+            const int64_t n = idx(ix, iy, iz, ny, nz);
+            if (!g.boundary[n]) continue;
+            double nm[3] = {0.0, 0.0, 0.0};
+            int count = 0;
+            for (int q = 1; q < kQ; ++q) {
+              const int64_t jx = ix + kE[q][0], jy = iy + kE[q][1], jz = iz + kE[q][2];
+              if (jx >= 0 && jx < nx && jy >= 0 && jy < ny && jz >= 0 && jz < nz &&
+                  g.solid[idx(jx, jy, jz, ny, nz)]) {
+                nm[0] -= kE[q][0];
+                nm[1] -= kE[q][1];
+                nm[2] -= kE[q][2];
+                ++count;
+              }
+            }
+            if (count > 0) {
+              for (int d = 0; d < 3; ++d) nm[d] /= count;
+              const double norm = std::sqrt(nm[0] * nm[0] + nm[1] * nm[1] + nm[2] * nm[2]);
+              if (norm > 1e-10)
+                for (int d = 0; d < 3; ++d) nm[d] /= norm;
+            }
+            for (int d = 0; d < 3; ++d) g.wall_normal[d * N + n] = (float)nm[d];
+          }
+    }
+    // Near-wall distance: 11 synchronous passes of periodic face-neighbour
+    // min-plus from the boundary nodes (fe_wetting.py:280-292) equal the
+    // face-graph distance capped at 11 (else 100); computed by breadth-first
+    // search from all boundary nodes at once.
+    std::vector<int64_t> frontier, next;
+    for (int64_t n = 0; n < N; ++n)
+      if (g.boundary[n]) {
+        g.dist[n] = 0;
+        frontier.push_back(n);
+      }
+    for (int pass = 1; pass <= kNearWallPasses && !frontier.empty(); ++pass) {
+      next.clear();
+      for (int64_t n : frontier) {
+        const int64_t iz = n % nz, t = n / nz, iy = t % ny, ix = t / ny;
+        const int64_t nb[6] = {idx(wrap(ix - 1, nx), iy, iz, ny, nz), idx(wrap(ix + 1, nx), iy, iz, ny, nz),
+                               idx(ix, wrap(iy - 1, ny), iz, ny, nz), idx(ix, wrap(iy + 1, ny), iz, ny, nz),
+                               idx(ix, iy, wrap(iz - 1, nz), ny, nz), idx(ix, iy, wrap(iz + 1, nz), ny, nz)};
+        for (int64_t m : nb)
+          if (g.dist[m] == 100) {
+            g.dist[m] = pass;
+            next.push_back(m);
+          }
+      }
+      frontier.swap(next);
+    }
+    // wall weight exp(-dist / (xi/2)) in float32, 0 in solid (fe_wetting.py:295-303)
+    float lut[kWwCodes];
+    near_wall_weights(lut);
+    for (int64_t n = 0; n < N; ++n) {
+      if (g.solid[n]) {
+        g.dist[n] = 100;
+        g.wall_weight[n] = 0.0f;
+      } else {
+        g.wall_weight[n] = lut[g.dist[n] <= kNearWallPasses ? g.dist[n] : kWwFarCode];
+        g.near_wall[n] = g.dist[n] < 10 ? 1 : 0;  // dist < 2 xi
+      }
+    }
+    // top-surface flag of the boundary-phi relaxation, |n_z| / |n| > 1/2 in
+    // the solver precision (fe_ac_solver.py:602-606)
+    for (int64_t n = 0; n < N; ++n) {
+      if (!g.boundary[n]) continue;
+      const float a = g.wall_normal[n], b = g.wall_normal[N + n], c = g.wall_normal[2 * N + n];
+      bool top;
+      if (dbl_precision) {
+        const double x = a, y = b, z = c;
+        double m = std::sqrt((x * x + y * y) + z * z);
+        if (m < 1e-10) m = 1e-10;
+        top = std::fabs(z) / m > 0.5;
+      } else {
+        float m = std::sqrt((a * a + b * b) + c * c);
+        if (m < 1e-10f) m = 1e-10f;
+        top = std::fabs(c) / m > 0.5f;
+      }
+      g.top[n] = top ? 1 : 0;
+    }
+  }
+  // node-class byte
+  g.cls.assign(N, 0);
+  for (int64_t n = 0; n < N; ++n) {
+    uint8_t c = 0;
+    if (g.solid[n]) c |= 1;
+    if (g.boundary[n]) c |= 2;
+    if (g.partial[n]) c |= 4;
+    if (g.top[n]) c |= 8;
+    int code;
+    if (g.solid[n]) code = kWwSolidCode;
+    else if (wetting && g.dist[n] <= kNearWallPasses) code = g.dist[n];
+    else code = kWwFarCode;
+    c |= (uint8_t)(code << 4);
+    g.cls[n] = c;
+  }
+  return 0;
+}
+
+void near_wall_weights(float* lut) {
+  // exp(-d / 2.5) in float32 for d = 0..11, d = 100 (code 12) and 0 for solid
+  // (code 13).  float32 exp of torch is correctly rounded on these inputs;
+  // the double exp rounded once to float reproduces it.
+  for (int d = 0; d <= kNearWallPasses; ++d) {
+    const float x = (-(float)d) / 2.5f;
+    lut[d] = (float)std::exp((double)x);
+  }
+  lut[kWwFarCode] = (float)std::exp((double)((-100.0f) / 2.5f));
+  lut[kWwSolidCode] = 0.0f;
+  lut[14] = 0.0f;
+  lut[15] = 0.0f;
+}
+
+}  // namespace lbm

@@ -1,0 +1,79 @@
+"""Build liblbm_gb300.so in-tree for sm_103a.
+
+Three translation units compiled in parallel and linked with nvcc:
+  csrc/lbm_kernels.cu   device kernels (nvcc, sm_103a)
+  csrc/lbm_capi.cu      the C ABI of include/lbm_gb300.h (nvcc host code)
+  csrc/lbm_geometry.cpp host geometry precompute (g++, -ffp-contract=off so
+                        the float sequences match numpy bit for bit)
+Output: lbm/_lib/liblbm_gb300.so next to this file.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(ROOT, "csrc")
+INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
+OUT_DIR = os.path.join(PKG, "_lib")
+LIB = os.path.join(OUT_DIR, "liblbm_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST_FLAGS = "-fPIC,-ffp-contract=off"
+
+
+def _nvcc():
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    return cand if os.path.exists(cand) else (shutil.which("nvcc") or "nvcc")
+
+
+def _sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                  if f.endswith((".cu", ".cpp", ".cuh", ".h")))
+
+
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = _sources() + [os.path.join(INCLUDE, "lbm_gb300.h"), os.path.abspath(__file__)]
+    return any(os.path.getmtime(p) > t for p in deps)
+
+
+def build(force=False, verbose=False):
+    """Compile the library if a source is newer than it; return its path."""
+    if not force and not _stale():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    obj_dir = os.path.join(OUT_DIR, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
+    nvcc = _nvcc()
+    common = ["-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC]
+    jobs = []
+    for src in ("lbm_kernels.cu", "lbm_capi.cu"):
+        obj = os.path.join(obj_dir, src + ".o")
+        jobs.append([nvcc, *common, *ARCH, "-lineinfo", "-Xcompiler", HOST_FLAGS, "-c",
+                     os.path.join(CSRC, src), "-o", obj])
+    obj = os.path.join(obj_dir, "lbm_geometry.cpp.o")
+    jobs.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
+                 "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, "lbm_geometry.cpp"), "-o", obj])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode:
+            raise RuntimeError("compile failed: " + " ".join(cmd[-3:]))
+
+    with ThreadPoolExecutor(len(jobs)) as ex:
+        list(ex.map(run, jobs))
+    objs = [j[-1] for j in jobs]
+    tmp = LIB + ".tmp"
+    run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,369 @@
+"""AllenCahnSolver: drop-in front end of the GB300 Allen-Cahn phase-field LBM.
+
+Same constructor, methods and readable attributes as the reference class
+(pytorch-lbm ``lbm/fe_ac_solver.py:51-732``): ``FEConfig`` in,
+``set_solid(solid_mask, solid_fraction=None)``, ``init_fields(phi, u=None)``,
+``step()``, and the fields ``phi, rho, u, P, p, mu_phi, f, g, solid,
+step_count, t, phi_mass_init, wetting``.  Every time step runs on the GPU
+through the C ABI of ``liblbm_gb300.so`` (two hand-written sm_103a kernels per
+step, see csrc/lbm_kernels.cu); there is no CPU path.
+
+Fields are produced on demand: the device keeps only the state the next step
+needs (post-collision populations, velocity, the previous phi) and a read of
+``solver.phi`` etc. launches a small read-out kernel that reproduces the value
+the reference holds after the same step.  Each read returns a new tensor.
+
+Options the reference implements but this solver does not yet cover
+(``interface_mode='cahn-hilliard'``, ``mu_drive > 0``, ``direct_wetting``,
+per-node ``geo_amplification`` tensors, 2-D grids) raise
+``NotImplementedError`` instead of running a different model.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .lattice import D3Q19
+
+_STAB = {"fakhari": 0, "liang": 1, "none": 2}
+
+
+def _host_array(x, dtype):
+    if torch.is_tensor(x):
+        x = x.detach().cpu().numpy()
+    return np.ascontiguousarray(np.asarray(x), dtype=dtype)
+
+
+class WettingTables:
+    """Read-only view of the wetting precompute (the attributes of the
+    reference's ConningtonLeeWetting that callers read:
+    lbm/fe_wetting.py:140,147,305-306), as device tensors."""
+
+    def __init__(self, solver, mode, tables):
+        dev = solver.device
+        self.mode = mode
+        self.is_boundary = torch.from_numpy(tables["is_boundary"]).to(dev)
+        self.wall_normal = torch.from_numpy(tables["wall_normal"]).to(dev)
+        self.wall_weight = torch.from_numpy(tables["wall_weight"]).to(dev)
+        self.near_wall_mask = torch.from_numpy(tables["near_wall"]).to(dev)
+        cfg = solver.config
+        self.theta_deg = cfg.theta_eq
+        self.kappa = cfg.kappa
+        self.sigma = cfg.sigma
+        self.phi_c = cfg.phi_c
+        self._geo_amplification = solver._geo_amplification
+        if mode == "linear":
+            h = cfg.sigma * math.cos(math.radians(cfg.theta_eq))
+            gs = solver._ghost_scale
+            if gs is None:
+                gs = 3.0 if abs(cfg.theta_eq - 90.0) > 60.0 else 2.0
+            self._h = h
+            self._ghost_scale = gs
+            self._h_over_kappa = h / cfg.kappa * gs
+            self._mu_wall = -h * 2.0
+        else:
+            self._phi_c_over_kappa = cfg.phi_c / cfg.kappa
+            self._h = self._h_over_kappa = self._mu_wall = 0.0
+
+
+class AllenCahnSolver:
+    """Conservative Allen-Cahn + pressure-velocity NS LBM on one GB300."""
+
+    def __init__(self, config, dtype=torch.float64, stab_mode="auto", mu_drive=0.0,
+                 boundary_relax=0.3, interface_mode="allen-cahn", ghost_scale=None,
+                 sharpen_reduce=0.8, mu_wall_scale=1.0, geometric_wetting=False,
+                 direct_wetting=False, ch_wall_blend=0.0, geo_amplification=1.0, ac_scale=1.0):
+        if config.nz == 1:
+            raise NotImplementedError("2-D (D2Q9) grids are not supported by the GB300 solver")
+        if interface_mode != "allen-cahn":
+            raise NotImplementedError("interface_mode='cahn-hilliard' is not supported")
+        if mu_drive and mu_drive > 0.0:
+            raise NotImplementedError("mu_drive > 0 is not supported")
+        if direct_wetting:
+            raise NotImplementedError("direct_wetting is not supported")
+        if torch.is_tensor(geo_amplification) or isinstance(geo_amplification, np.ndarray):
+            raise NotImplementedError("per-node geo_amplification is not supported")
+        if dtype not in (torch.float32, torch.float64):
+            raise ValueError("dtype must be torch.float32 or torch.float64")
+        self.config = config
+        dev = torch.device(config.device) if not isinstance(config.device, torch.device) else config.device
+        if dev.type != "cuda":
+            raise RuntimeError("the GB300 solver runs on a CUDA device only (config.device='cuda')")
+        if not torch.cuda.is_available():
+            raise RuntimeError("no CUDA device is available; the GB300 solver has no CPU fallback")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        self.dtype = dtype
+        self.step_count = 0
+        self.t = 0.0
+        self.stab_mode = "fakhari" if stab_mode == "auto" else stab_mode
+        if self.stab_mode not in _STAB:
+            raise ValueError(f"unknown stab_mode {stab_mode!r}")
+        self.mu_drive = mu_drive
+        self.boundary_relax = boundary_relax
+        self.interface_mode = interface_mode
+        self._ghost_scale = ghost_scale
+        self._sharpen_reduce = sharpen_reduce
+        self._mu_wall_scale = mu_wall_scale
+        self.geometric_wetting = geometric_wetting
+        self.direct_wetting = direct_wetting
+        self.ch_wall_blend = ch_wall_blend
+        self._geo_amplification = geo_amplification
+        self._ac_scale = ac_scale
+        self.shape = tuple(config.grid_shape)
+        self.ndim = 3
+        self.lattice = D3Q19()
+        self.cs2 = self.lattice.cs2
+        self._tau_f = config.tau_h if config.tau_h > 0 else config.tau_l
+        self._tau_g = config.tau_g
+        self._mobility = self.cs2 * (self._tau_f - 0.5)
+        self.solid = torch.zeros(self.shape, dtype=torch.bool, device=dev)
+        self.wetting = None
+        self.bounce_back = None
+        self.solid_fraction = None
+        self._has_partial = False
+        self._phi_wall_target = None
+        if config.theta_eq != 90.0:
+            c = math.cos(math.radians(config.theta_eq))
+            disc = 1.0 - 4.0 * (-c / 3.0)
+            self._phi_wall_target = (0.5 * (1.0 - math.sqrt(disc)) if disc >= 0 else
+                                     0.5 * (1.0 - math.cos(math.pi - math.radians(config.theta_eq))))
+        self._prec = nat.LBM_F32 if dtype == torch.float32 else nat.LBM_F64
+        p = nat.LbmParams()
+        for k in ("rho_l", "rho_g", "sigma", "xi", "beta", "kappa", "phi_c", "tau_l", "tau_g",
+                  "tau_h", "theta_eq"):
+            setattr(p, k, float(getattr(config, k)))
+        gf = tuple(config.g_force[:3]) + (0.0,) * (3 - len(config.g_force[:3]))
+        p.g_force = (ctypes.c_double * 3)(*[float(x) for x in gf])
+        p.boundary_relax = float(boundary_relax)
+        p.sharpen_reduce = float(sharpen_reduce)
+        p.mu_wall_scale = float(mu_wall_scale)
+        p.geo_amplification = float(geo_amplification)
+        p.ac_scale = float(ac_scale)
+        p.ghost_scale = float(ghost_scale) if ghost_scale is not None else 0.0
+        p.stab_mode = _STAB[self.stab_mode]
+        p.geometric_wetting = 1 if geometric_wetting else 0
+        self._params = p
+        self._lib = nat.lib()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(dev):
+            nat.check(self._lib.lbm_create(ctypes.byref(p), self.shape[0], self.shape[1], self.shape[2],
+                                           self._prec, ctypes.byref(h)), "lbm_create")
+        self._h = h
+        self._geometry_set = False
+        self._initialized = False
+        self._cache = {}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.lbm_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -- setup ----------------------------------------------------------------
+    def set_solid(self, solid_mask, solid_fraction=None):
+        """lbm/fe_ac_solver.py:193-237 (geometry precompute in the native library)."""
+        solid = _host_array(solid_mask, np.bool_)
+        if solid.shape != self.shape:
+            raise ValueError(f"solid mask shape {solid.shape} != grid {self.shape}")
+        frac = None
+        fdt = nat.LBM_DT_NONE
+        if solid_fraction is not None:
+            fr = solid_fraction.detach().cpu().numpy() if torch.is_tensor(solid_fraction) else np.asarray(solid_fraction)
+            if fr.dtype == np.float32:
+                frac, fdt = np.ascontiguousarray(fr), nat.LBM_DT_F32
+            else:
+                frac, fdt = np.ascontiguousarray(fr, dtype=np.float64), nat.LBM_DT_F64
+            if frac.shape != self.shape:
+                raise ValueError(f"solid fraction shape {frac.shape} != grid {self.shape}")
+        s8 = solid.view(np.uint8)
+        nat.check(self._lib.lbm_set_geometry(self._h, s8.ctypes.data_as(ctypes.c_void_p),
+                                             frac.ctypes.data_as(ctypes.c_void_p) if frac is not None else None,
+                                             fdt), "lbm_set_geometry")
+        self._geometry_set = True
+        self.solid = torch.from_numpy(solid.copy()).to(self.device)
+        self._solid_any = bool(solid.any())
+        if frac is not None:
+            self.solid_fraction = torch.tensor(frac, dtype=self.dtype, device=self.device)
+        tables = self._geometry_tables()
+        self._partial_mask = torch.from_numpy(tables["partial"]).to(self.device)
+        self._has_partial = bool(tables["partial"].any())
+        cfg = self.config
+        if cfg.theta_eq != 90.0 and cfg.kappa > 0:
+            mode = "linear" if cfg.theta_eq > 130.0 or cfg.theta_eq < 50.0 else "quadratic"
+            self.wetting = WettingTables(self, mode, tables)
+        else:
+            self.wetting = None
+        self._cache.clear()
+
+    def _geometry_tables(self):
+        N = int(np.prod(self.shape))
+        out = dict(node_class=np.empty(N, np.uint8), is_boundary=np.empty(N, np.bool_),
+                   wall_normal=np.empty((3, N), np.float32), wall_weight=np.empty(N, np.float32),
+                   near_wall=np.empty(N, np.bool_), partial=np.empty(N, np.bool_))
+        c = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        nat.check(self._lib.lbm_get_geometry(self._h, c(out["node_class"]), c(out["is_boundary"]),
+                                             c(out["wall_normal"]), c(out["wall_weight"]),
+                                             c(out["near_wall"]), c(out["partial"])), "lbm_get_geometry")
+        return {k: v.reshape((3,) + self.shape if k == "wall_normal" else self.shape) for k, v in out.items()}
+
+    def init_fields(self, phi_init, u_init=None):
+        """lbm/fe_ac_solver.py:239-261."""
+        if not self._geometry_set:
+            # the reference allows init before set_solid (no solid nodes)
+            self.set_solid(np.zeros(self.shape, dtype=bool))
+        stream = nat.stream_ptr()
+        if torch.is_tensor(phi_init) and phi_init.is_cuda:
+            src_dt = torch.float32 if phi_init.dtype == torch.float32 else torch.float64
+            phi_d = phi_init.detach().to(device=self.device, dtype=src_dt).contiguous()
+            u_d = (u_init.detach().to(device=self.device, dtype=src_dt).contiguous()
+                   if u_init is not None else None)
+            self._keep = (phi_d, u_d)
+            nat.check(self._lib.lbm_init_fields(self._h, nat.ptr(phi_d), nat.ptr(u_d),
+                                                nat.LBM_DT_F32 if src_dt == torch.float32 else nat.LBM_DT_F64,
+                                                1, stream), "lbm_init_fields")
+        else:
+            ph = phi_init.detach().cpu().numpy() if torch.is_tensor(phi_init) else np.asarray(phi_init)
+            npdt = np.float32 if ph.dtype == np.float32 else np.float64
+            ph = np.ascontiguousarray(ph, dtype=npdt)
+            if ph.shape != self.shape:
+                raise ValueError(f"phi shape {ph.shape} != grid {self.shape}")
+            uh = None
+            if u_init is not None:
+                uh = u_init.detach().cpu().numpy() if torch.is_tensor(u_init) else np.asarray(u_init)
+                uh = np.ascontiguousarray(uh, dtype=npdt)
+                if uh.shape != (3,) + self.shape:
+                    raise ValueError(f"u shape {uh.shape} != (3,) + grid")
+            # host sources are copied asynchronously: keep them alive until the copy ran
+            self._keep = (ph, uh)
+            nat.check(self._lib.lbm_init_fields(
+                self._h, ph.ctypes.data_as(ctypes.c_void_p),
+                uh.ctypes.data_as(ctypes.c_void_p) if uh is not None else None,
+                nat.LBM_DT_F32 if npdt == np.float32 else nat.LBM_DT_F64, 0, stream), "lbm_init_fields")
+            torch.cuda.current_stream().synchronize()
+        self._keep = None
+        self._initialized = True
+        self.step_count = 0
+        self.t = 0.0
+        self._cache.clear()
+
+    # -- time stepping --------------------------------------------------------
+    def step(self):
+        """One time step (lbm/fe_ac_solver.py:380-639); asynchronous on the
+        current CUDA stream."""
+        self.run(1)
+
+    def run(self, nsteps, stream=None):
+        """``nsteps`` time steps in one call."""
+        if not self._initialized:
+            raise RuntimeError("init_fields must be called before step()")
+        nat.check(self._lib.lbm_step(self._h, int(nsteps), nat.stream_ptr(stream)), "lbm_step")
+        self.step_count += int(nsteps)
+        self.t += float(nsteps)
+        self._cache.clear()
+
+    # -- fields ---------------------------------------------------------------
+    def _fields(self, want):
+        missing = [k for k in want if k not in self._cache]
+        if missing:
+            if not self._initialized:
+                raise RuntimeError("fields are defined after init_fields")
+            bits = {"phi": nat.FIELD_PHI, "rho": nat.FIELD_RHO, "u": nat.FIELD_U, "P": nat.FIELD_P,
+                    "p": nat.FIELD_PRESS, "mu_phi": nat.FIELD_MU}
+            mask = 0
+            out = {}
+            for k in missing:
+                shp = (3,) + self.shape if k == "u" else self.shape
+                out[k] = torch.empty(shp, dtype=self.dtype, device=self.device)
+                mask |= bits[k]
+            nat.check(self._lib.lbm_get_fields(
+                self._h, mask, nat.ptr(out.get("phi")), nat.ptr(out.get("rho")), nat.ptr(out.get("u")),
+                nat.ptr(out.get("P")), nat.ptr(out.get("p")), nat.ptr(out.get("mu_phi")),
+                nat.stream_ptr()), "lbm_get_fields")
+            self._cache.update(out)
+        return [self._cache[k] for k in want]
+
+    @property
+    def phi(self):
+        return self._fields(["phi"])[0]
+
+    @property
+    def rho(self):
+        return self._fields(["rho"])[0]
+
+    @property
+    def u(self):
+        return self._fields(["u"])[0]
+
+    @property
+    def P(self):
+        return self._fields(["P"])[0]
+
+    @property
+    def p(self):
+        return self._fields(["p"])[0]
+
+    @property
+    def mu_phi(self):
+        return self._fields(["mu_phi"])[0]
+
+    def fields(self, *names):
+        """Several fields from one read-out launch, e.g. ``fields('phi', 'u')``."""
+        return self._fields(list(names))
+
+    def _populations(self):
+        if "f" not in self._cache:
+            Q = 19
+            f = torch.empty((Q,) + self.shape, dtype=self.dtype, device=self.device)
+            g = torch.empty_like(f)
+            nat.check(self._lib.lbm_get_populations(self._h, nat.ptr(f), nat.ptr(g), nat.stream_ptr()),
+                      "lbm_get_populations")
+            self._cache["f"], self._cache["g"] = f, g
+        return self._cache["f"], self._cache["g"]
+
+    @property
+    def f(self):
+        return self._populations()[0]
+
+    @property
+    def g(self):
+        return self._populations()[1]
+
+    @property
+    def phi_mass_init(self):
+        if not self._initialized:
+            return None
+        m = ctypes.c_double()
+        nat.check(self._lib.lbm_get_scalars(self._h, ctypes.byref(m), None, None, None), "lbm_get_scalars")
+        return float(m.value)
+
+    def scalars(self):
+        """(phi_mass_init, last sum(phi), last mass-correction factor, steps)."""
+        a, b, c, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+        nat.check(self._lib.lbm_get_scalars(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                            ctypes.byref(n)), "lbm_get_scalars")
+        return a.value, b.value, c.value, n.value
+
+    def measure(self, stream=None):
+        """Spread diagnostics of the current phi, reduced on the device:
+        volume, C_max, Dx, Dy, Dz, k, z_com, count, has_nan."""
+        out = (ctypes.c_double * 9)()
+        nat.check(self._lib.lbm_measure(self._h, out, nat.stream_ptr(stream)), "lbm_measure")
+        keys = ("volume", "C_max", "Dx", "Dy", "Dz", "k", "z_com", "count", "has_nan")
+        d = dict(zip(keys, list(out)))
+        d["count"] = int(d["count"])
+        d["has_nan"] = bool(d["has_nan"])
+        return d
+
+    def status(self):
+        v = ctypes.c_uint32()
+        nat.check(self._lib.lbm_status(self._h, ctypes.byref(v)), "lbm_status")
+        return int(v.value)
