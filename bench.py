@@ -17,7 +17,7 @@ One "step" is one lattice time step of the whole grid.  Reported:
              host numpy arrays: construction, set_solid, init_fields (H2D),
              K steps, the sweep drivers' read of phi to host every 50 steps
              (D2H), final spread measurement.
-  roofline   the dominant kernel (k_collide): algorithmic bytes per launch /
+  roofline   the step kernel (k_step, one launch per step): algorithmic bytes per launch /
              its CUDA-event duration, against the measured HBM copy peak.
   cpu_baseline  the numpy oracle (oracle/ac_oracle.py) on a bounded sample of
              the same workload, one host core.
@@ -44,11 +44,8 @@ import numpy as np  # noqa: E402
 # populations), u (3) and the previous phi (1), each read once and written
 # once: 2 x 4 x (38 + 3 + 1) = 336 B.
 B_ALG_STEP = 336
-# k_collide reads those 168 B plus this step's phi (4 B) and the node class
-# byte, and writes the 168 B.
-B_ALG_COLLIDE = 341
-# k_phi reads f (76 B) and the class byte and writes phi (4 B).
-B_ALG_PHI = 81
+# The fused step kernel k_step moves those 336 B plus the node-class byte.
+B_ALG_KERNEL = 337
 
 WORKLOADS = {
     "ridge150": dict(grid=(150, 150, 107), substrate=("ridge", 1.0, 22.5), center=(75, 75, 80),
@@ -230,7 +227,7 @@ def run_ours(args, rank, world, device):
         torch.cuda.synchronize(device)
     barrier(world)
     s.step_count += K
-    phi_ms, col_ms, tot_ms = float(ms3[0]), float(ms3[1]), float(ms3[2])
+    ker_ms, tot_ms = float(ms3[1]), float(ms3[2])
     tot_ms = max_over_ranks(tot_ms, world, device)
     status = s.status()
     meas = s.measure()
@@ -262,9 +259,9 @@ def run_ours(args, rank, world, device):
     out = None
     if rank == 0:
         peak, peak_kind = peaks()
-        col_s = col_ms / K / 1e3
-        achieved = B_ALG_COLLIDE * n / col_s / 1e9
-        traffic_pn = profiled_traffic("k_collide")
+        ker_s = ker_ms / K / 1e3
+        achieved = B_ALG_KERNEL * n / ker_s / 1e9
+        traffic_pn = profiled_traffic("k_step")
         step_bw = B_ALG_STEP * n / (tot_ms / K / 1e3) / 1e9
         w = WORKLOADS[name]
         cpu = None
@@ -287,12 +284,11 @@ def run_ours(args, rank, world, device):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic_pn * n if traffic_pn is not None else None,
-                         "kernel": "k_collide", "bytes_per_node": B_ALG_COLLIDE,
-                         "ms_per_launch": col_ms / K},
+                         "kernel": "k_step", "bytes_per_node": B_ALG_KERNEL,
+                         "ms_per_launch": ker_ms / K},
             "step_roofline": {"achieved_gbs": step_bw, "bytes_per_node": B_ALG_STEP, "peak": peak,
-                              "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / B_ALG_STEP,
-                              "k_phi_ms": phi_ms / K, "k_collide_ms": col_ms / K},
-            "gpu_launches": 2 * K,
+                              "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / B_ALG_STEP},
+            "gpu_launches": K,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "spread_after": {k2: meas[k2] for k2 in ("Dx", "Dy", "k", "z_com", "volume")},

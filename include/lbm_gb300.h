@@ -111,12 +111,17 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
  * (lbm/fe_ac_solver.py:380-639).  Asynchronous on `stream`; no host sync. */
 int lbm_step(LbmHandle* h, int nsteps, void* stream);
 
-/* As lbm_step, with CUDA events recorded on `stream` around each of the two
- * kernels of every step; on return (synchronised) kernel_ms[0] and
- * kernel_ms[1] hold the summed durations of the phi-recovery and collision
- * kernels and kernel_ms[2] the whole span.  For measurement; same results as
- * lbm_step. */
+/* As lbm_step, with CUDA events recorded on `stream` around the step kernel
+ * launches; on return (synchronised) kernel_ms3[1] holds their summed
+ * duration, kernel_ms3[2] the whole span and kernel_ms3[0] zero.  For
+ * measurement; same results as lbm_step. */
 int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3);
+
+/* Tile extents (x, y, z) of the fused step kernel; 0 = automatic, else 2..64
+ * for x and y and 2..256 for z.  Results do not depend on the tiling; speed
+ * does.  No reference counterpart (a GB300 launch parameter). */
+int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz);
+int lbm_get_tile(LbmHandle* h, int* txyz3);
 
 /* Write the fields the reference exposes after the last step (or after
  * init) into caller device buffers of the handle's precision.  `mask` selects

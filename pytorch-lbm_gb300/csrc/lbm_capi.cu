@@ -17,7 +17,9 @@
 
 namespace lbm {
 template <typename T>
-cudaError_t launch_step(const Consts<T>&, const State<T>&, bool, bool, cudaStream_t, cudaEvent_t);
+size_t step_smem_bytes(const Tiling&);
+template <typename T>
+cudaError_t launch_step(const Consts<T>&, const State<T>&, const Tiling&, bool, bool, cudaStream_t);
 template <typename T, typename S>
 cudaError_t launch_init(const Consts<T>&, const State<T>&, const S*, const S*, cudaStream_t);
 template <typename T>
@@ -59,9 +61,7 @@ struct LbmHandle {
   void* f[2] = {nullptr, nullptr};
   void* g[2] = {nullptr, nullptr};
   void* u = nullptr;
-  void* phi = nullptr;
-  void* phi_prev = nullptr;
-  void* relax = nullptr;
+  void* phi[2] = {nullptr, nullptr};  // phi recovered by the last two steps
   void* eps = nullptr;
   uint8_t* cls = nullptr;
   float* wn = nullptr;
@@ -77,7 +77,9 @@ struct LbmHandle {
   Geometry geo;
   // sequencing
   bool geometry_set = false, initialized = false;
+  Tiling tiling{};
   int cur = 0;            // buffer index holding the current state
+  int pc = 0;             // phi buffer holding the latest recovered phi
   bool raw = true;        // current state is the reference state itself (after init)
   bool first = true;      // phi*u of the previous step does not exist yet
   int c_last = 0;         // cbuf slot of the last step's correction
@@ -105,9 +107,13 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
     k.wc[q] = (T)wf / (T)cs2;
     k.w2c[q] = (T)2 * k.wc[q];
     k.wac[q] = (T)ac_coeff * (T)wf;
+    k.wac3[q] = k.wac[q] / (T)cs2;
   }
   k.cs2 = (T)cs2;
   k.two_cs2 = (T)(2.0 * cs2);
+  k.inv_cs2 = (T)1 / k.cs2;
+  k.inv_two_cs2 = (T)1 / k.two_cs2;
+  k.inv_W = (T)1 / (T)p.xi;
   k.beta4 = (T)(4.0 * p.beta);
   k.kappa = (T)p.kappa;
   k.phi_c = (T)p.phi_c;
@@ -118,6 +124,7 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   k.drho = (T)(p.rho_l - p.rho_g);
   k.visc = (T)((0.5 - p.tau_g) / p.tau_g);
   k.omega_f = (T)(1.0 / tau_f);
+  k.omega_g = (T)1 / (T)p.tau_l;
   k.tau_l = (T)p.tau_l;
   k.tl_m = (T)(p.tau_l - 0.5);
   k.tg_m = (T)(p.tau_g - 0.5);
@@ -169,8 +176,9 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   return k;
 }
 
+// State of a step reading population buffer `in_buf` and phi buffer `phi_in`.
 template <typename T>
-State<T> make_state(const LbmHandle& h, int in_buf) {
+State<T> make_state(const LbmHandle& h, int in_buf, int phi_in) {
   State<T> s;
   std::memset(&s, 0, sizeof(s));
   s.fin = static_cast<const T*>(h.f[in_buf]);
@@ -178,9 +186,8 @@ State<T> make_state(const LbmHandle& h, int in_buf) {
   s.fout = static_cast<T*>(h.f[in_buf ^ 1]);
   s.gout = static_cast<T*>(h.g[in_buf ^ 1]);
   s.u = static_cast<T*>(h.u);
-  s.phi_prev = static_cast<T*>(h.phi_prev);
-  s.phi = static_cast<T*>(h.phi);
-  s.relax = static_cast<T*>(h.relax);
+  s.phi_in = static_cast<const T*>(h.phi[phi_in]);
+  s.phi_out = static_cast<T*>(h.phi[phi_in ^ 1]);
   s.cls = h.cls;
   s.wn = h.wn;
   s.eps = static_cast<const T*>(h.eps);
@@ -192,8 +199,35 @@ State<T> make_state(const LbmHandle& h, int in_buf) {
   return s;
 }
 
+// Tiling of the fused step: z extent near 48 (balanced over nz), x and y
+// extents giving ~2.3k nodes per tile.
+Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz) {
+  if (tz <= 0) {
+    const int ntz = (int)((nz + 47) / 48);
+    tz = (int)((nz + ntz - 1) / ntz);
+  }
+  if (tx <= 0 || ty <= 0) {
+    int side = (int)std::lround(std::sqrt(2304.0 / tz));
+    side = std::max(2, std::min(side, 16));
+    if (tx <= 0) tx = side;
+    if (ty <= 0) ty = side;
+  }
+  Tiling t;
+  tx = std::max(tx, 2);
+  ty = std::max(ty, 2);
+  tz = std::max(tz, 2);
+  t.tx = (int)std::min<int64_t>(tx, nx);
+  t.ty = (int)std::min<int64_t>(ty, ny);
+  t.tz = (int)std::min<int64_t>(tz, nz);
+  t.ntx = (int)((nx + t.tx - 1) / t.tx);
+  t.nty = (int)((ny + t.ty - 1) / t.ty);
+  t.ntz = (int)((nz + t.tz - 1) / t.tz);
+  t.hmax = (t.tx + 2) * (t.ty + 2) * (t.tz + 2);
+  return t;
+}
+
 void free_all(LbmHandle* h) {
-  void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u, h->phi, h->phi_prev, h->relax, h->eps,
+  void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u, h->phi[0], h->phi[1], h->eps,
                   h->cls, h->wn, h->partials, h->counters, h->cbuf, h->scal, h->meas_phi};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -210,19 +244,20 @@ template <typename T>
 int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr) {
   const Consts<T>& k = consts_of<T>(*h);
   for (int i = 0; i < nsteps; ++i) {
-    State<T> s = make_state<T>(*h, h->cur);
+    State<T> s = make_state<T>(*h, h->cur, h->pc);
     s.c_prev = h->c_last;
     s.c_cur = h->c_last ^ 1;
-    if (ev) CUDA_TRY(cudaEventRecord(ev[2 * i], st));
-    CUDA_TRY(launch_step<T>(k, s, h->raw, h->first, st, ev ? ev[2 * i + 1] : nullptr));
+    if (ev) CUDA_TRY(cudaEventRecord(ev[i], st));
+    CUDA_TRY(launch_step<T>(k, s, h->tiling, h->raw, h->first, st));
     h->last_raw_in = h->raw;
     h->cur ^= 1;
+    h->pc ^= 1;
     h->c_last ^= 1;
     h->raw = false;
     h->first = false;
     ++h->steps;
   }
-  if (ev) CUDA_TRY(cudaEventRecord(ev[2 * nsteps], st));
+  if (ev) CUDA_TRY(cudaEventRecord(ev[nsteps], st));
   return LBM_OK;
 }
 
@@ -256,8 +291,12 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   h->wetting = params->theta_eq != 90.0 && params->kappa > 0;
   cudaGetDevice(&h->device);
   const size_t T = h->tsize;
+  h->tiling = make_tiling(nx, ny, nz, 0, 0, 0);
+  // per-block partial sums: init (one block per 256 nodes), step (one per
+  // tile; tile extents are at least 2) and measure
   const int nblocks = (int)((N + kBlock - 1) / kBlock);
-  const size_t npart = std::max<size_t>((size_t)nblocks, (size_t)kMeasureBlocks * kMeasVals);
+  const size_t max_tiles = (size_t)((nx + 1) / 2) * (size_t)((ny + 1) / 2) * (size_t)((nz + 1) / 2);
+  const size_t npart = std::max<size_t>({(size_t)nblocks, max_tiles, (size_t)kMeasureBlocks * kMeasVals});
   cudaError_t e = cudaSuccess;
   auto A = [&](void** p, size_t bytes) {
     if (e == cudaSuccess) e = cudaMalloc(p, bytes);
@@ -267,9 +306,8 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
     A(&h->g[b], (size_t)Q * N * T);
   }
   A(&h->u, 3 * N * T);
-  A(&h->phi, N * T);
-  A(&h->phi_prev, N * T);
-  A(&h->relax, N * T);
+  A(&h->phi[0], N * T);
+  A(&h->phi[1], N * T);
   A(&h->eps, N * T);
   A((void**)&h->cls, N);
   A((void**)&h->wn, 3 * N * sizeof(float));
@@ -345,12 +383,12 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
   }
   cudaError_t e;
   if (h->prec == LBM_F32) {
-    State<float> s = make_state<float>(*h, in);
+    State<float> s = make_state<float>(*h, in, h->pc ^ 1);
     e = src_dtype == LBM_DT_F32
             ? launch_init<float, float>(h->kf, s, (const float*)dphi, (const float*)du, st)
             : launch_init<float, double>(h->kf, s, (const double*)dphi, (const double*)du, st);
   } else {
-    State<double> s = make_state<double>(*h, in);
+    State<double> s = make_state<double>(*h, in, h->pc ^ 1);
     e = src_dtype == LBM_DT_F32
             ? launch_init<double, float>(h->kd, s, (const float*)dphi, (const float*)du, st)
             : launch_init<double, double>(h->kd, s, (const double*)dphi, (const double*)du, st);
@@ -378,27 +416,39 @@ int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3)
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_step_profiled: call lbm_init_fields first");
   if (nsteps <= 0) return fail(LBM_E_ARG, "lbm_step_profiled: nsteps must be positive");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  std::vector<cudaEvent_t> ev(2 * (size_t)nsteps + 1, nullptr);
+  std::vector<cudaEvent_t> ev((size_t)nsteps + 1, nullptr);
   for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
   int rc = h->prec == LBM_F32 ? do_step<float>(h, nsteps, st, ev.data()) : do_step<double>(h, nsteps, st, ev.data());
-  float a = 0.f, b = 0.f, tot = 0.f;
+  float tot = 0.f;
   if (rc == LBM_OK) {
     cudaError_t e = cudaEventSynchronize(ev.back());
-    for (int i = 0; i < nsteps && e == cudaSuccess; ++i) {
-      float x = 0.f, y = 0.f;
-      e = cudaEventElapsedTime(&x, ev[2 * i], ev[2 * i + 1]);
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&y, ev[2 * i + 1], ev[2 * i + 2]);
-      a += x;
-      b += y;
-    }
     if (e == cudaSuccess) e = cudaEventElapsedTime(&tot, ev.front(), ev.back());
     if (e != cudaSuccess) rc = fail(LBM_E_CUDA, std::string("lbm_step_profiled: ") + cudaGetErrorString(e));
   }
   for (auto& e : ev) cudaEventDestroy(e);
-  kernel_ms3[0] = a;
-  kernel_ms3[1] = b;
+  kernel_ms3[0] = 0.f;
+  kernel_ms3[1] = tot;
   kernel_ms3[2] = tot;
   return rc;
+}
+
+int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz) {
+  if (!h) return fail(LBM_E_ARG, "lbm_set_tile: null handle");
+  if (tx == 1 || ty == 1 || tz == 1 || tx < 0 || ty < 0 || tz < 0 || tx > 64 || ty > 64 || tz > 256)
+    return fail(LBM_E_ARG, "lbm_set_tile: tile extents must be in [2, 64] x [2, 64] x [2, 256] (0 = automatic)");
+  Tiling t = make_tiling(h->nx, h->ny, h->nz, tx, ty, tz);
+  const size_t sm = h->prec == LBM_F32 ? step_smem_bytes<float>(t) : step_smem_bytes<double>(t);
+  if (sm > 200 * 1024) return fail(LBM_E_ARG, "lbm_set_tile: tile too large for shared memory");
+  h->tiling = t;
+  return LBM_OK;
+}
+
+int lbm_get_tile(LbmHandle* h, int* txyz3) {
+  if (!h || !txyz3) return fail(LBM_E_ARG, "lbm_get_tile: null argument");
+  txyz3[0] = h->tiling.tx;
+  txyz3[1] = h->tiling.ty;
+  txyz3[2] = h->tiling.tz;
+  return LBM_OK;
 }
 
 int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u, void* P, void* p, void* mu,
@@ -412,13 +462,14 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u, v
   const int mode = h->steps == 0 ? 0 : 1;
   const int in_buf = h->steps == 0 ? h->cur : (h->cur ^ 1);  // the last step's input buffer
   cudaError_t e;
+  // phi_out of the state = the latest recovered phi
   if (h->prec == LBM_F32) {
-    State<float> s = make_state<float>(*h, in_buf);
+    State<float> s = make_state<float>(*h, in_buf, h->pc ^ 1);
     s.c_cur = h->c_last;
     e = launch_observe<float>(h->kf, s, h->last_raw_in, mask, mode, (float*)phi, (float*)rho, (float*)u,
                               (float*)P, (float*)p, (float*)mu, st);
   } else {
-    State<double> s = make_state<double>(*h, in_buf);
+    State<double> s = make_state<double>(*h, in_buf, h->pc ^ 1);
     s.c_cur = h->c_last;
     e = launch_observe<double>(h->kd, s, h->last_raw_in, mask, mode, (double*)phi, (double*)rho, (double*)u,
                                (double*)P, (double*)p, (double*)mu, st);
@@ -432,13 +483,14 @@ int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream) {
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_get_populations: not initialised");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
+  // fin = the current state, phi_in = the latest phi, c_prev = its correction
   if (h->prec == LBM_F32) {
-    State<float> s = make_state<float>(*h, h->cur);
-    s.c_cur = h->c_last;
+    State<float> s = make_state<float>(*h, h->cur, h->pc);
+    s.c_prev = h->c_last;
     e = launch_populations<float>(h->kf, s, h->raw, (float*)f, (float*)g, st);
   } else {
-    State<double> s = make_state<double>(*h, h->cur);
-    s.c_cur = h->c_last;
+    State<double> s = make_state<double>(*h, h->cur, h->pc);
+    s.c_prev = h->c_last;
     e = launch_populations<double>(h->kd, s, h->raw, (double*)f, (double*)g, st);
   }
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_get_populations: ") + cudaGetErrorString(e));

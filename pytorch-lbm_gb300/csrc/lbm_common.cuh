@@ -50,6 +50,21 @@ struct Nbr {
   }
 };
 
+__device__ __forceinline__ Nbr make_nbr_xyz(int ix, int iy, int iz, int nx, int ny, int nz) {
+  const int sx = ny * nz, sy = nz;
+  Nbr b;
+  b.ox[0] = ix == 0 ? (nx - 1) * sx : -sx;
+  b.ox[1] = 0;
+  b.ox[2] = ix == nx - 1 ? -(nx - 1) * sx : sx;
+  b.oy[0] = iy == 0 ? (ny - 1) * sy : -sy;
+  b.oy[1] = 0;
+  b.oy[2] = iy == ny - 1 ? -(ny - 1) * sy : sy;
+  b.oz[0] = iz == 0 ? nz - 1 : -1;
+  b.oz[1] = 0;
+  b.oz[2] = iz == nz - 1 ? -(nz - 1) : 1;
+  return b;
+}
+
 __device__ __forceinline__ Nbr make_nbr(int n, int nx, int ny, int nz, int* ix_out, int* iy_out,
                                         int* iz_out) {
   const int iz = n % nz;
@@ -83,11 +98,13 @@ struct Consts {
   T wc[Q];     // w_i / cs2                      (stencil weights)
   T w2c[Q];    // 2 w_i / cs2                    (laplacian weights)
   T wac[Q];    // (1 - 1/(2 tau_f)) w_i          (Allen-Cahn source)
-  T cs2, two_cs2;
+  T wac3[Q];   // wac_i / cs2
+  T cs2, two_cs2, inv_cs2, inv_two_cs2, inv_W;
   T beta4, kappa, phi_c, W;
   T rho_l, rho_g, rho_floor, drho;
   T visc;      // (1/2 - tau_g) / tau_g
   T omega_f;   // 1 / tau_f
+  T omega_g;   // 1 / tau_l (tau_l == tau_g)
   T tau_l, tl_m, tg_m;  // tau_l, tau_l - 1/2, tau_g - 1/2
   int tau_const;        // tau_l == tau_g
   T gforce[3];
@@ -111,9 +128,8 @@ struct State {
   T* fout;        // post-collision populations written this step
   T* gout;
   T* u;           // velocity [3][N], in place
-  T* phi_prev;    // phi of the last step (phi*u of the last step = phi_prev*u)
-  T* phi;         // phi of this step (written by the phi kernel)
-  T* relax;       // boundary-phi relaxation: pending phi target / scale, -1 = none
+  const T* phi_in;  // phi recovered by the last step (before its mass correction)
+  T* phi_out;       // phi recovered by this step
   const uint8_t* cls;
   const float* wn;  // wall normal [3][N] (non-zero at boundary nodes only)
   const T* eps;     // solid fraction (read at partial nodes only)
@@ -123,6 +139,14 @@ struct State {
   double* scal;     // [0] phi_mass_init, [1] last sum(phi)
   unsigned* status;
   int c_prev, c_cur;  // cbuf slots: factor applied to fin, factor produced this step
+};
+
+// Tiling of the fused step kernel: one CTA per tile of TX x TY x TZ nodes
+// (z fastest), tiles clipped at the domain edge.
+struct Tiling {
+  int tx, ty, tz;     // tile extents
+  int ntx, nty, ntz;  // tiles per axis
+  int hmax;           // (tx + 2)(ty + 2)(tz + 2): halo-tile nodes
 };
 
 }  // namespace lbm

@@ -3,21 +3,27 @@
 // State convention ("pull" form).  Between steps the population buffers hold
 // POST-COLLISION values F(x, q) of every node, solid and partial nodes
 // included.  The reference's state at the start of a step (pytorch-lbm
-// lbm/fe_ac_solver.py:548-591: streamed, bounced back at solid nodes,
+// lbm/fe_ac_solver.py:548-636: streamed, bounced back at solid nodes,
 // volume-penalised at partial nodes, scaled by the global phi-mass correction
 // c, then boundary-phi relaxed at active boundary nodes) is reconstructed on
 // read:
-//   fluid x    f(x,q) = c F(x - e_q, q)                       (periodic)
-//   solid x    f(x,q) = c F(x, opp q)                          (:556-566)
+//   fluid x    f(x,q) = c F(x - e_q, q)                               (periodic)
+//   solid x    f(x,q) = c F(x, opp q)                                  (:556-566)
 //   partial x  f(x,q) = c ((1 - eps) F(x - e_q, q) + eps F(x, opp q))  (:569-578)
-//   relaxed x  f(x,q) *= clamp(phi_new / max(sum_q f(x,q), 1e-10), 1/2, 2)  (:620-636)
-// g is reconstructed the same way without c and without relaxation.  Right
-// after init (RAW) the buffers hold the reference state itself.
+//   relaxed x  f(x,q) *= clamp(phi_new / max(sum_q f(x,q), 1e-10), 1/2, 2)   (:594-636)
+// where the relaxation target phi_new is recomputed from the previous step's
+// phi and c (it depends on nothing else).  g is reconstructed the same way
+// without c and without relaxation.  Right after init (RAW) the buffers hold
+// the reference state itself.
 //
-// One step = two launches: k_phi (phi recovery + deterministic global sum ->
-// c) and k_collide (stencils, wetting, forces, velocity, Allen-Cahn source,
-// both BGK collisions, relaxation bookkeeping).  Arithmetic follows the
-// reference's operation order; sums run in population order.
+// One step = ONE launch of k_step.  Each CTA owns a tile of nodes: phase A
+// recovers phi on the tile plus a one-node halo into shared memory (pulling
+// f), phase B runs the stencils, wetting, forces, velocity, Allen-Cahn source
+// and both BGK collisions for the tile's nodes (pulling f again, from L1/L2,
+// and g).  The grid-wide sum of phi that gives the next mass correction is a
+// deterministic last-block reduction of the per-tile partial sums.
+// Arithmetic follows the reference's operation order; sums run in population
+// order; the isotropic gradient is accumulated without FMA contraction.
 #include <cuda_runtime.h>
 
 #include "lbm_common.cuh"
@@ -35,12 +41,29 @@ __device__ __forceinline__ T ldg(const T* p) {
   return __ldg(p);
 }
 
+// Separately rounded multiply and add (never contracted into an FMA).  The
+// isotropic gradient is accumulated with these so that mirror-symmetric
+// neighbour pairs cancel to exactly zero, as in the reference: the
+// sharpening normal grad/|grad| is otherwise set by an FMA's rounding residue
+// at the points where the gradient vanishes.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rcp(float a) { return 1.0f / a; }
+__device__ __forceinline__ double rcp(double a) { return 1.0 / a; }
+
+// q = floor(t / d) for 0 <= t < 2^22 via a float reciprocal: the relative
+// error of (t + 1/2) * (1/d) is below 2^-23, inside the 1/(2d) margin.
+__device__ __forceinline__ int fdiv(int t, float inv_d) { return (int)(((float)t + 0.5f) * inv_d); }
+
 // Block-wide sum of a double; result valid in thread 0.
 __device__ __forceinline__ double block_sum(double v) {
   __shared__ double s_warp[kBlock / 32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
   if (lane == 0) s_warp[wid] = v;
   __syncthreads();
   double r = 0.0;
@@ -66,7 +89,6 @@ __device__ __forceinline__ bool last_block_total(double part, double* partials, 
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
-  // The last block reduces the partials with all its threads, in a fixed order.
   double acc = 0.0;
   for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc += ((volatile double*)partials)[i];
   acc = block_sum(acc);
@@ -114,6 +136,16 @@ __device__ __forceinline__ T seqsum(const T (&v)[Q]) {
   return s;
 }
 
+// Boundary-phi relaxation target of a top-surface boundary node from the
+// previous step's phi and mass correction (lbm/fe_ac_solver.py:594-624);
+// negative when the node is not active.
+template <typename T>
+__device__ __forceinline__ T relax_target(const Consts<T>& k, T phi_prev, T corr) {
+  const T pb = clamp01(phi_prev * corr);
+  if (pb > T(0.15) && pb < T(0.85)) return clamp01(pb + k.relax_r * (k.relax_target - pb));
+  return T(-1);
+}
+
 // Relaxation scale of lbm/fe_ac_solver.py:626-629.
 template <typename T>
 __device__ __forceinline__ T relax_scale(T target, T sum_f) {
@@ -122,71 +154,36 @@ __device__ __forceinline__ T relax_scale(T target, T sum_f) {
   return s < T(0.5) ? T(0.5) : (s > T(2.0) ? T(2.0) : s);
 }
 
-// ---------------------------------------------------------------------------
-// K1: phi recovery, sum(phi) and the mass-correction factor
-// ---------------------------------------------------------------------------
+// f at node n as the reference holds it at the start of the step.
 template <typename T, bool RAW>
-__global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T> s) {
-  const int n = blockIdx.x * kBlock + threadIdx.x;
-  const size_t N = (size_t)k.N;
-  double part = 0.0;
-  if (n < k.N) {
-    const uint8_t c = s.cls[n];
-    T phi = T(0);
-    if (!(c & kSolid)) {
-      int ix, iy, iz;
-      const Nbr nb = make_nbr(n, k.nx, k.ny, k.nz, &ix, &iy, &iz);
-      const T eps = (c & kPartial) ? s.eps[n] : T(0);
-      T v[Q];
-      fetch_pop<T, RAW, !RAW>(v, s.fin, n, N, nb, c, eps, RAW ? T(1) : s.cbuf[s.c_prev]);
-      if (!RAW && (c & kTop)) {
-        const T r = s.relax[n];
-        if (r >= T(0)) {
-          const T sc = relax_scale(r, seqsum(v));
+__device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const State<T>& s, int n, size_t N,
+                                        const Nbr& nb, uint8_t c, T eps) {
+  const T corr = RAW ? T(1) : s.cbuf[s.c_prev];
+  fetch_pop<T, RAW, !RAW>(v, s.fin, n, N, nb, c, eps, corr);
+  if (!RAW && k.relax_on && (c & kTop)) {
+    const T r = relax_target(k, ldg(s.phi_in + n), corr);
+    if (r >= T(0)) {
+      const T sc = relax_scale(r, seqsum(v));
 #pragma unroll
-          for (int q = 0; q < Q; ++q) v[q] = v[q] * sc;
-          s.relax[n] = sc;  // k_collide applies the same scale
-        }
-      }
-      phi = clamp01(seqsum(v));
+      for (int q = 0; q < Q; ++q) v[q] = v[q] * sc;
     }
-    s.phi[n] = phi;
-    part = (double)phi;
-  }
-  part = block_sum(part);
-  double total;
-  if (last_block_total(part, s.partials, s.counter, &total)) {
-    // lbm/fe_ac_solver.py:582-589, in T: c = (1/max(S,1e-6)) * M0 if S > 1e-6 else 1
-    const T S = (T)total;
-    T corr = T(1);
-    if (S > T(1e-6)) {
-      const T safe = S < T(1e-6) ? T(1e-6) : S;
-      corr = (T(1) / safe) * (T)s.scal[0];
-    } else {
-      atomicOr(s.status, 2u);
-    }
-    if (!(total == total) || total - total != 0.0) atomicOr(s.status, 1u);
-    s.cbuf[s.c_cur] = corr;
-    s.scal[1] = total;
   }
 }
 
 // ---------------------------------------------------------------------------
 // Isotropic gradient / laplacian with the ghost-node wetting correction
-// (lbm/fe_ac_solver.py:296-320 fused, :282-294 unfused; fe_wetting.py:418-446)
+// (lbm/fe_ac_solver.py:296-320 fused, :282-294 unfused; fe_wetting.py:418-446).
+// ps[q] holds phi(x + e_q); nsolid(q) tells whether that neighbour is solid.
 // ---------------------------------------------------------------------------
-template <typename T, bool FUSED>
-__device__ __forceinline__ void stencil(const Consts<T>& k, const State<T>& s, int n, const Nbr& nb,
-                                        uint8_t c, T phi, T& gx, T& gy, T& gz, T& lap) {
-  T ps[Q];
-#pragma unroll
-  for (int q = 1; q < Q; ++q) ps[q] = ldg(s.phi + nb.at(n, ex(q), ey(q), ez(q)));
+template <typename T, bool FUSED, typename SolidFn>
+__device__ __forceinline__ void grad_lap(const Consts<T>& k, const State<T>& s, int n, uint8_t c, T phi,
+                                         T (&ps)[Q], SolidFn nsolid, T& gx, T& gy, T& gz, T& lap) {
   if (k.wetting && (c & kBoundary)) {
     const size_t N = (size_t)k.N;
     const float n0 = s.wn[n], n1 = s.wn[N + n], n2 = s.wn[2 * N + n];
 #pragma unroll
     for (int q = 1; q < Q; ++q) {
-      if (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) {
+      if (nsolid(q)) {
         float nde = 0.0f;
         nde = __fadd_rn(nde, __fmul_rn(n0, (float)ex(q)));
         nde = __fadd_rn(nde, __fmul_rn(n1, (float)ey(q)));
@@ -202,9 +199,9 @@ __device__ __forceinline__ void stencil(const Consts<T>& k, const State<T>& s, i
   gx = gy = gz = lap = T(0);
 #pragma unroll
   for (int q = 1; q < Q; ++q) {
-    if (ex(q) != 0) gx = gx + (ex(q) > 0 ? k.wc[q] : -k.wc[q]) * ps[q];
-    if (ey(q) != 0) gy = gy + (ey(q) > 0 ? k.wc[q] : -k.wc[q]) * ps[q];
-    if (ez(q) != 0) gz = gz + (ez(q) > 0 ? k.wc[q] : -k.wc[q]) * ps[q];
+    if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
+    if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
+    if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
     if (FUSED) {
       lap = lap + k.w2c[q] * (ps[q] - phi);
     } else {
@@ -224,26 +221,27 @@ __device__ __forceinline__ T chem_pot(const Consts<T>& k, uint8_t c, T phi, T la
   return mu;
 }
 
+// e_q . (a0, a1, a2) with the reference's exact two-term sums.
+template <typename T>
+__device__ __forceinline__ T edot(int q, T a0, T a1, T a2) {
+  T r = T(0);
+  bool any = false;
+  if (ex(q) != 0) { r = ex(q) > 0 ? a0 : -a0; any = true; }
+  if (ey(q) != 0) { const T t = ey(q) > 0 ? a1 : -a1; r = any ? r + t : t; any = true; }
+  if (ez(q) != 0) { const T t = ez(q) > 0 ? a2 : -a2; r = any ? r + t : t; }
+  return r;
+}
+
 // ---------------------------------------------------------------------------
-// K2: fused stencil + wetting + forces + velocity + source + collisions
+// The collision of one node (lbm/fe_ac_solver.py:392-530), given its phi,
+// gradient and laplacian; writes fout, gout, u, phi_out.
 // ---------------------------------------------------------------------------
 template <typename T, bool RAW, bool FIRST>
-__global__ void __launch_bounds__(kBlock) k_collide(Consts<T> k, State<T> s) {
-  const int n = blockIdx.x * kBlock + threadIdx.x;
-  if (n >= k.N) return;
+__device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>& s, int n, const Nbr& nb,
+                                             uint8_t c, T phi, T gx, T gy, T gz, T lap) {
   const size_t N = (size_t)k.N;
-  const uint8_t c = s.cls[n];
-  int ix, iy, iz;
-  const Nbr nb = make_nbr(n, k.nx, k.ny, k.nz, &ix, &iy, &iz);
-  const T phi = s.phi[n];  // clamped, 0 in solid; phi_safe == phi
-
-  // 2. density
   const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
-
-  // gradient, laplacian, chemical potential
-  T gx, gy, gz, lap;
-  stencil<T, true>(k, s, n, nb, c, phi, gx, gy, gz, lap);
   const T mu = chem_pot(k, c, phi, lap);
 
   // geometric contact-angle gradient correction (fe_wetting.py:448-539).  The
@@ -251,22 +249,22 @@ __global__ void __launch_bounds__(kBlock) k_collide(Consts<T> k, State<T> s) {
   // identity, so only boundary nodes are visited.
   if (k.geometric && (c & kBoundary)) {
     const T n0 = (T)s.wn[n], n1 = (T)s.wn[N + n], n2 = (T)s.wn[2 * N + n];
-    const T gn = (n0 * gx + n1 * gy) + n2 * gz;
-    const T tx = gx - gn * n0, ty = gy - gn * n1, tz = gz - gn * n2;
-    T tm = sqrt((tx * tx + ty * ty) + tz * tz);
+    const T gn = add_rn(add_rn(mul_rn(n0, gx), mul_rn(n1, gy)), mul_rn(n2, gz));
+    const T tx = gx - mul_rn(gn, n0), ty = gy - mul_rn(gn, n1), tz = gz - mul_rn(gn, n2);
+    T tm = sqrt(add_rn(add_rn(mul_rn(tx, tx), mul_rn(ty, ty)), mul_rn(tz, tz)));
     tm = tm < T(1e-10) ? T(1e-10) : tm;
-    T gd = ((-tm) * k.cos_t) / k.sin_t;
+    T gd = mul_rn(-tm, k.cos_t) / k.sin_t;
     if (k.amp_active) {
       const T delta = gd - gn;
-      gd = gn + delta * k.amp;
+      gd = add_rn(gn, mul_rn(delta, k.amp));
     }
-    const T cx = tx + gd * n0, cy = ty + gd * n1, cz = tz + gd * n2;
-    const T gm = sqrt((gx * gx + gy * gy) + gz * gz);
+    const T cx = add_rn(tx, mul_rn(gd, n0)), cy = add_rn(ty, mul_rn(gd, n1)), cz = add_rn(tz, mul_rn(gd, n2));
+    const T gm = sqrt(add_rn(add_rn(mul_rn(gx, gx), mul_rn(gy, gy)), mul_rn(gz, gz)));
     if (gm > T(1e-6)) {
       const T bl = k.ww[c >> kWwShift];
-      gx = gx + bl * (cx - gx);
-      gy = gy + bl * (cy - gy);
-      gz = gz + bl * (cz - gz);
+      gx = add_rn(gx, mul_rn(bl, cx - gx));
+      gy = add_rn(gy, mul_rn(bl, cy - gy));
+      gz = add_rn(gz, mul_rn(bl, cz - gz));
     }
   }
 
@@ -280,19 +278,13 @@ __global__ void __launch_bounds__(kBlock) k_collide(Consts<T> k, State<T> s) {
   const T uo0 = s.u[n], uo1 = s.u[N + n], uo2 = s.u[2 * N + n];
   T sxx, syy, szz, sxy, sxz, syz;
   {
-    const T usq = (uo0 * uo0 + uo1 * uo1) + uo2 * uo2;
-    const T b = usq / k.two_cs2;
+    const T b = ((uo0 * uo0 + uo1 * uo1) + uo2 * uo2) * k.inv_two_cs2;
     bool fxx = true, fyy = true, fzz = true, fxy = true, fxz = true, fyz = true;
     sxx = syy = szz = sxy = sxz = syz = T(0);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      T eu = T(0);
-      bool any = false;
-      if (ex(q) != 0) { eu = ex(q) > 0 ? uo0 : -uo0; any = true; }
-      if (ey(q) != 0) { const T t = ey(q) > 0 ? uo1 : -uo1; eu = any ? eu + t : t; any = true; }
-      if (ez(q) != 0) { const T t = ez(q) > 0 ? uo2 : -uo2; eu = any ? eu + t : t; any = true; }
-      const T ec = eu / k.cs2;
-      const T sq = k.w[q] * ((ec + ec * ec / T(2)) - b);
+      const T ec = edot(q, uo0, uo1, uo2) * k.inv_cs2;
+      const T sq = k.w[q] * ((ec + ec * ec * T(0.5)) - b);
       const T gneq = g[q] - (P * k.w[q] + sq);
       if (ex(q) != 0) { sxx = fxx ? gneq : sxx + gneq; fxx = false; }
       if (ey(q) != 0) { syy = fyy ? gneq : syy + gneq; fyy = false; }
@@ -304,30 +296,22 @@ __global__ void __launch_bounds__(kBlock) k_collide(Consts<T> k, State<T> s) {
   }
 
   // 5. forces (Fakhari 2017, :416-439)
-  T F0, F1, F2;
-  {
+  T F0 = mu * gx, F1 = mu * gy, F2 = mu * gz;
+  if (k.stab_mode <= 1) {
     const T fp = ((-P) * k.drho) * k.cs2;
-    const T m0 = (sxx * gx + sxy * gy) + sxz * gz;
-    const T m1 = (sxy * gx + syy * gy) + syz * gz;
-    const T m2 = (sxz * gx + syz * gy) + szz * gz;
-    F0 = mu * gx;
-    F1 = mu * gy;
-    F2 = mu * gz;
-    if (k.stab_mode <= 1) {
-      F0 = F0 + fp * gx;
-      F1 = F1 + fp * gy;
-      F2 = F2 + fp * gz;
-    }
-    if (k.stab_mode == 0) {
-      F0 = F0 + (k.visc * m0) * k.drho;
-      F1 = F1 + (k.visc * m1) * k.drho;
-      F2 = F2 + (k.visc * m2) * k.drho;
-    }
-    if (k.has_gforce) {
-      F0 = F0 + k.gforce[0] * rho;
-      F1 = F1 + k.gforce[1] * rho;
-      F2 = F2 + k.gforce[2] * rho;
-    }
+    F0 = F0 + fp * gx;
+    F1 = F1 + fp * gy;
+    F2 = F2 + fp * gz;
+  }
+  if (k.stab_mode == 0) {
+    F0 = F0 + (k.visc * ((sxx * gx + sxy * gy) + sxz * gz)) * k.drho;
+    F1 = F1 + (k.visc * ((sxy * gx + syy * gy) + syz * gz)) * k.drho;
+    F2 = F2 + (k.visc * ((sxz * gx + syz * gy) + szz * gz)) * k.drho;
+  }
+  if (k.has_gforce) {
+    F0 = F0 + k.gforce[0] * rho;
+    F1 = F1 + k.gforce[1] * rho;
+    F2 = F2 + k.gforce[2] * rho;
   }
 
   // 6. velocity (:442-447)
@@ -341,9 +325,10 @@ __global__ void __launch_bounds__(kBlock) k_collide(Consts<T> k, State<T> s) {
       if (ey(q) != 0) { const T t = ey(q) > 0 ? g[q] : -g[q]; u1 = f1 ? t : u1 + t; f1 = false; }
       if (ez(q) != 0) { const T t = ez(q) > 0 ? g[q] : -g[q]; u2 = f2 ? t : u2 + t; f2 = false; }
     }
-    u0 = u0 + (T(0.5) * F0) / rho_eff;
-    u1 = u1 + (T(0.5) * F1) / rho_eff;
-    u2 = u2 + (T(0.5) * F2) / rho_eff;
+    const T hr = T(0.5) * rcp(rho_eff);
+    u0 = u0 + F0 * hr;
+    u1 = u1 + F1 * hr;
+    u2 = u2 + F2 * hr;
     if (c & kSolid) u0 = u1 = u2 = T(0);
   }
 
@@ -352,104 +337,144 @@ __global__ void __launch_bounds__(kBlock) k_collide(Consts<T> k, State<T> s) {
   {
     T d0 = T(0), d1 = T(0), d2 = T(0);
     if (!FIRST) {
-      const T pp = s.phi_prev[n];
+      const T pp = s.phi_in[n];
       d0 = phi * u0 - pp * uo0;
       d1 = phi * u1 - pp * uo1;
       d2 = phi * u2 - pp * uo2;
     }
     T gm = sqrt((gx * gx + gy * gy) + gz * gz);
     gm = gm < T(1e-10) ? T(1e-10) : gm;
-    const T lam = ((T(4) * phi) * (T(1) - phi)) / k.W;
-    const T cl = k.cs2 * lam;
-    T sh0 = ((cl * (gx / gm)) * k.ac_scale);
-    T sh1 = ((cl * (gy / gm)) * k.ac_scale);
-    T sh2 = ((cl * (gz / gm)) * k.ac_scale);
-    if (k.wetting) {
-      const T fac = T(1) - k.sharpen_reduce * k.ww[c >> kWwShift];
-      sh0 = sh0 * fac;
-      sh1 = sh1 * fac;
-      sh2 = sh2 * fac;
-    }
-    S0 = d0 + sh0;
-    S1 = d1 + sh1;
-    S2 = d2 + sh2;
+    const T lam = ((T(4) * phi) * (T(1) - phi)) * k.inv_W;
+    T cl = k.cs2 * lam * k.ac_scale * rcp(gm);
+    if (k.wetting) cl = cl * (T(1) - k.sharpen_reduce * k.ww[c >> kWwShift]);
+    S0 = d0 + cl * gx;
+    S1 = d1 + cl * gy;
+    S2 = d2 + cl * gz;
   }
 
   // 8. collisions (:496-530)
-  const T usq = (u0 * u0 + u1 * u1) + u2 * u2;
-  const T b = usq / k.two_cs2;
+  const T b = ((u0 * u0 + u1 * u1) + u2 * u2) * k.inv_two_cs2;
   {
     T f[Q];
-    fetch_pop<T, RAW, !RAW>(f, s.fin, n, N, nb, c, eps, RAW ? T(1) : s.cbuf[s.c_prev]);
-    if (!RAW && (c & kTop)) {
-      const T sc = s.relax[n];
-      if (sc >= T(0)) {
-#pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = f[q] * sc;
-      }
-    }
+    fetch_f<T, RAW>(f, k, s, n, N, nb, c, eps);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      T eu = T(0), es = T(0);
-      bool any = false;
-      if (ex(q) != 0) { eu = ex(q) > 0 ? u0 : -u0; es = ex(q) > 0 ? S0 : -S0; any = true; }
-      if (ey(q) != 0) {
-        const T t = ey(q) > 0 ? u1 : -u1, ts = ey(q) > 0 ? S1 : -S1;
-        eu = any ? eu + t : t; es = any ? es + ts : ts; any = true;
-      }
-      if (ez(q) != 0) {
-        const T t = ez(q) > 0 ? u2 : -u2, ts = ez(q) > 0 ? S2 : -S2;
-        eu = any ? eu + t : t; es = any ? es + ts : ts; any = true;
-      }
-      const T ec = eu / k.cs2;
-      const T feq = phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b));
-      const T src = (k.wac[q] * es) / k.cs2;
+      const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
+      const T feq = phi * (k.w[q] * (((T(1) + ec) + ec * ec * T(0.5)) - b));
+      const T src = k.wac3[q] * edot(q, S0, S1, S2);
       s.fout[(size_t)q * N + n] = (f[q] - k.omega_f * (f[q] - feq)) + src;
     }
   }
   {
-    T tau;
+    T om;
     if (k.tau_const) {
-      tau = k.tau_l;
+      om = k.omega_g;
     } else {
       const T eta = phi * k.rho_l * k.tl_m + (T(1) - phi) * k.rho_g * k.tg_m;
       const T rden = phi * k.rho_l + (T(1) - phi) * k.rho_g;
-      tau = T(0.5) + eta / rden;
+      om = rcp(T(0.5) + eta / rden);
     }
-    const T rcp = T(1) / tau;
-    const T ns = T(1) - rcp * T(0.5);
-    const T den = rho_eff * k.cs2;
+    const T nsd = (T(1) - om * T(0.5)) * rcp(rho_eff * k.cs2);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      T eu = T(0), eF = T(0);
-      bool any = false;
-      if (ex(q) != 0) { eu = ex(q) > 0 ? u0 : -u0; eF = ex(q) > 0 ? F0 : -F0; any = true; }
-      if (ey(q) != 0) {
-        const T t = ey(q) > 0 ? u1 : -u1, tf = ey(q) > 0 ? F1 : -F1;
-        eu = any ? eu + t : t; eF = any ? eF + tf : tf; any = true;
-      }
-      if (ez(q) != 0) {
-        const T t = ez(q) > 0 ? u2 : -u2, tf = ez(q) > 0 ? F2 : -F2;
-        eu = any ? eu + t : t; eF = any ? eF + tf : tf; any = true;
-      }
-      const T ec = eu / k.cs2;
-      const T sq = k.w[q] * ((ec + ec * ec / T(2)) - b);
-      const T geq = P * k.w[q] + sq;
-      const T G = ((ns * k.w[q]) * eF) / den;
-      s.gout[(size_t)q * N + n] = (g[q] - rcp * (g[q] - geq)) + G;
+      const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
+      const T geq = P * k.w[q] + k.w[q] * ((ec + ec * ec * T(0.5)) - b);
+      const T G = (nsd * k.w[q]) * edot(q, F0, F1, F2);
+      s.gout[(size_t)q * N + n] = (g[q] - om * (g[q] - geq)) + G;
     }
   }
   s.u[n] = u0;
   s.u[N + n] = u1;
   s.u[2 * N + n] = u2;
-  s.phi_prev[n] = phi;
+  s.phi_out[n] = phi;
+}
 
-  // 12. boundary-phi relaxation target for the next step (:594-624)
-  if (k.relax_on && (c & kTop)) {
-    const T pb = clamp01(phi * s.cbuf[s.c_cur]);
-    T r = T(-1);
-    if (pb > T(0.15) && pb < T(0.85)) r = clamp01(pb + k.relax_r * (k.relax_target - pb));
-    s.relax[n] = r;
+// ---------------------------------------------------------------------------
+// The fused time step
+// ---------------------------------------------------------------------------
+template <typename T, bool RAW, bool FIRST>
+__global__ void __launch_bounds__(kBlock) k_step(Consts<T> k, State<T> s, Tiling tl) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* sphi = reinterpret_cast<T*>(smem);
+  uint8_t* scls = reinterpret_cast<uint8_t*>(sphi + tl.hmax);
+  const size_t N = (size_t)k.N;
+
+  // tile of this CTA, clipped at the domain edge
+  const int b = blockIdx.x;
+  const int bz = b % tl.ntz, byx = b / tl.ntz;
+  const int by = byx % tl.nty, bx = byx / tl.nty;
+  const int x0 = bx * tl.tx, y0 = by * tl.ty, z0 = bz * tl.tz;
+  const int ex_ = min(tl.tx, k.nx - x0), ey_ = min(tl.ty, k.ny - y0), ez_ = min(tl.tz, k.nz - z0);
+  const int HY = ey_ + 2, HZ = ez_ + 2;
+  const int H = (ex_ + 2) * HY * HZ;
+  const float inv_hz = 1.0f / (float)HZ, inv_hy = 1.0f / (float)HY;
+
+  // phase A: phi on the tile and its halo
+  double part = 0.0;
+  for (int h = threadIdx.x; h < H; h += kBlock) {
+    const int r = fdiv(h, inv_hz);
+    const int hz = h - r * HZ;
+    const int hx = fdiv(r, inv_hy);
+    const int hy = r - hx * HY;
+    int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
+    gx = gx < 0 ? gx + k.nx : (gx >= k.nx ? gx - k.nx : gx);
+    gy = gy < 0 ? gy + k.ny : (gy >= k.ny ? gy - k.ny : gy);
+    gz = gz < 0 ? gz + k.nz : (gz >= k.nz ? gz - k.nz : gz);
+    const int n = (gx * k.ny + gy) * k.nz + gz;
+    const uint8_t c = s.cls[n];
+    T phi = T(0);
+    if (!(c & kSolid)) {
+      const Nbr nb = make_nbr_xyz(gx, gy, gz, k.nx, k.ny, k.nz);
+      const T eps = (c & kPartial) ? s.eps[n] : T(0);
+      T v[Q];
+      fetch_f<T, RAW>(v, k, s, n, N, nb, c, eps);
+      phi = clamp01(seqsum(v));
+    }
+    sphi[h] = phi;
+    scls[h] = c;
+    if (hx >= 1 && hx <= ex_ && hy >= 1 && hy <= ey_ && hz >= 1 && hz <= ez_) part += (double)phi;
+  }
+  __syncthreads();
+
+  // sum(phi) of the tile -> mass-correction factor of this step (:582-589)
+  part = block_sum(part);
+  double total;
+  if (last_block_total(part, s.partials, s.counter, &total)) {
+    const T S = (T)total;
+    T corr = T(1);
+    if (S > T(1e-6)) {
+      const T safe = S < T(1e-6) ? T(1e-6) : S;
+      corr = (T(1) / safe) * (T)s.scal[0];
+    } else {
+      atomicOr(s.status, 2u);
+    }
+    if (!(total == total) || total - total != 0.0) atomicOr(s.status, 1u);
+    s.cbuf[s.c_cur] = corr;
+    s.scal[1] = total;
+  }
+
+  // phase B: the tile's nodes
+  const int E = ex_ * ey_ * ez_;
+  const float inv_ez = 1.0f / (float)ez_, inv_ey = 1.0f / (float)ey_;
+  const int sx = HY * HZ;
+  for (int t = threadIdx.x; t < E; t += kBlock) {
+    const int r = fdiv(t, inv_ez);
+    const int lz = t - r * ez_;
+    const int lx = fdiv(r, inv_ey);
+    const int ly = r - lx * ey_;
+    const int h = ((lx + 1) * HY + (ly + 1)) * HZ + (lz + 1);
+    const int n = ((x0 + lx) * k.ny + (y0 + ly)) * k.nz + (z0 + lz);
+    const uint8_t c = scls[h];
+    const T phi = sphi[h];
+    T ps[Q];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) ps[q] = sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)];
+    T gx, gy, gz, lap;
+    grad_lap<T, true>(k, s, n, c, phi, ps,
+                      [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; },
+                      gx, gy, gz, lap);
+    const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
+    collide_node<T, RAW, FIRST>(k, s, n, nb, c, phi, gx, gy, gz, lap);
   }
 }
 
@@ -465,27 +490,19 @@ __global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T> s, const 
   if (n < k.N) {
     const T phi = clamp01((T)phi0[n]);
     const T v0 = u0 ? (T)u0[n] : T(0), v1 = u0 ? (T)u0[N + n] : T(0), v2 = u0 ? (T)u0[2 * N + n] : T(0);
-    const T usq = (v0 * v0 + v1 * v1) + v2 * v2;
-    const T b = usq / k.two_cs2;
+    const T b = ((v0 * v0 + v1 * v1) + v2 * v2) / k.two_cs2;
     T* f = const_cast<T*>(s.fin);
     T* g = const_cast<T*>(s.gin);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      T eu = T(0);
-      bool any = false;
-      if (ex(q) != 0) { eu = ex(q) > 0 ? v0 : -v0; any = true; }
-      if (ey(q) != 0) { const T t = ey(q) > 0 ? v1 : -v1; eu = any ? eu + t : t; any = true; }
-      if (ez(q) != 0) { const T t = ez(q) > 0 ? v2 : -v2; eu = any ? eu + t : t; any = true; }
-      const T ec = eu / k.cs2;
+      const T ec = edot(q, v0, v1, v2) / k.cs2;
       f[(size_t)q * N + n] = phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b));
       g[(size_t)q * N + n] = T(0) * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b);
     }
     s.u[n] = v0;
     s.u[N + n] = v1;
     s.u[2 * N + n] = v2;
-    s.phi[n] = phi;
-    s.phi_prev[n] = phi;
-    s.relax[n] = T(-1);
+    s.phi_out[n] = phi;
     part = (double)phi;
   }
   part = block_sum(part);
@@ -499,7 +516,8 @@ __global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T> s, const 
 }
 
 // ---------------------------------------------------------------------------
-// Field read-out (the reference's attribute values after the last step)
+// Field read-out (the reference's attribute values after the last step).
+// s.phi_out holds the last recovered phi, s.cbuf[s.c_cur] its correction.
 // ---------------------------------------------------------------------------
 enum ObserveMode { kObsInit = 0, kObsStep = 1 };
 
@@ -510,14 +528,15 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T> s, uns
   if (n >= k.N) return;
   const size_t N = (size_t)k.N;
   const uint8_t c = s.cls[n];
-  const T phi = s.phi[n];
+  const T phi = s.phi_out[n];
   const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
   if (mask & 1u) {
     T v = phi;
     if (mode == kObsStep) {
-      v = clamp01(phi * s.cbuf[s.c_cur]);
+      const T corr = s.cbuf[s.c_cur];
+      v = clamp01(phi * corr);
       if (k.relax_on && (c & kTop)) {
-        const T r = s.relax[n];
+        const T r = relax_target(k, phi, corr);
         if (r >= T(0)) v = r;
       }
     }
@@ -544,15 +563,20 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T> s, uns
       if (mask & 16u) p_o[n] = mode == kObsStep ? P * k.cs2 : rho * k.cs2;
     }
     if (mask & 32u) {
+      T ps[Q];
+#pragma unroll
+      for (int q = 1; q < Q; ++q) ps[q] = ldg(s.phi_out + nb.at(n, ex(q), ey(q), ez(q)));
+      auto nsolid = [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; };
       T gx, gy, gz, lap;
-      if (mode == kObsStep) stencil<T, true>(k, s, n, nb, c, phi, gx, gy, gz, lap);
-      else stencil<T, false>(k, s, n, nb, c, phi, gx, gy, gz, lap);
+      if (mode == kObsStep) grad_lap<T, true>(k, s, n, c, phi, ps, nsolid, gx, gy, gz, lap);
+      else grad_lap<T, false>(k, s, n, c, phi, ps, nsolid, gx, gy, gz, lap);
       mu_o[n] = chem_pot(k, c, phi, lap);
     }
   }
 }
 
-// Current populations in the reference layout.
+// Current populations in the reference layout: s.fin/s.gin hold the last
+// step's output, s.phi_in that step's phi and s.c_prev its correction.
 template <typename T, bool RAW>
 __global__ void __launch_bounds__(kBlock) k_populations(Consts<T> k, State<T> s, T* f_o, T* g_o) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
@@ -564,15 +588,7 @@ __global__ void __launch_bounds__(kBlock) k_populations(Consts<T> k, State<T> s,
   const T eps = (c & kPartial) ? s.eps[n] : T(0);
   T v[Q];
   if (f_o) {
-    fetch_pop<T, RAW, !RAW>(v, s.fin, n, N, nb, c, eps, RAW ? T(1) : s.cbuf[s.c_cur]);
-    if (!RAW && k.relax_on && (c & kTop)) {
-      const T r = s.relax[n];
-      if (r >= T(0)) {
-        const T sc = relax_scale(r, seqsum(v));
-#pragma unroll
-        for (int q = 0; q < Q; ++q) v[q] = v[q] * sc;
-      }
-    }
+    fetch_f<T, RAW>(v, k, s, n, N, nb, c, eps);
 #pragma unroll
     for (int q = 0; q < Q; ++q) f_o[(size_t)q * N + n] = v[q];
   }
@@ -589,6 +605,21 @@ __global__ void __launch_bounds__(kBlock) k_populations(Consts<T> k, State<T> s,
 // Partials per block: [sum, max, minx, maxx, miny, maxy, minz, maxz, sumz, count, nan]
 // ---------------------------------------------------------------------------
 constexpr int kMeasVals = 11;
+
+// r <- merge(r, q): sum, max, (min, max) x 3 axes, sum, sum, max
+template <typename A, typename B>
+__device__ __forceinline__ void meas_merge(A& r, const B& q) {
+  r[0] += q[0];
+  r[1] = fmax(r[1], (double)q[1]);
+#pragma unroll
+  for (int j = 2; j < 8; j += 2) {
+    r[j] = fmin(r[j], (double)q[j]);
+    r[j + 1] = fmax(r[j + 1], (double)q[j + 1]);
+  }
+  r[8] += q[8];
+  r[9] += q[9];
+  r[10] = fmax(r[10], (double)q[10]);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, const T* __restrict__ phi,
@@ -612,19 +643,12 @@ __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, cons
       v[9] += 1.0;
     }
   }
-  // warp reduce
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    v[0] += __shfl_down_sync(0xffffffffu, v[0], o);
-    v[1] = fmax(v[1], __shfl_down_sync(0xffffffffu, v[1], o));
+    double q[kMeasVals];
 #pragma unroll
-    for (int j = 2; j < 8; j += 2) {
-      v[j] = fmin(v[j], __shfl_down_sync(0xffffffffu, v[j], o));
-      v[j + 1] = fmax(v[j + 1], __shfl_down_sync(0xffffffffu, v[j + 1], o));
-    }
-    v[8] += __shfl_down_sync(0xffffffffu, v[8], o);
-    v[9] += __shfl_down_sync(0xffffffffu, v[9], o);
-    v[10] = fmax(v[10], __shfl_down_sync(0xffffffffu, v[10], o));
+    for (int j = 0; j < kMeasVals; ++j) q[j] = __shfl_down_sync(0xffffffffu, v[j], o);
+    meas_merge(v, q);
   }
   __shared__ double sw[kBlock / 32][kMeasVals];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -633,33 +657,36 @@ __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, cons
   __syncthreads();
   __shared__ bool s_last;
   if (threadIdx.x == 0) {
-    for (int w = 1; w < kBlock / 32; ++w) {
-      v[0] += sw[w][0];
-      v[1] = fmax(v[1], sw[w][1]);
-      for (int j = 2; j < 8; j += 2) { v[j] = fmin(v[j], sw[w][j]); v[j + 1] = fmax(v[j + 1], sw[w][j + 1]); }
-      v[8] += sw[w][8];
-      v[9] += sw[w][9];
-      v[10] = fmax(v[10], sw[w][10]);
-    }
+    for (int w = 1; w < kBlock / 32; ++w) meas_merge(v, sw[w]);
     for (int j = 0; j < kMeasVals; ++j) partials[(size_t)blockIdx.x * kMeasVals + j] = v[j];
     __threadfence();
     s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (s_last && threadIdx.x == 0) {
-    __threadfence();
-    volatile double* pp = partials;
-    double r[kMeasVals];
-    for (int j = 0; j < kMeasVals; ++j) r[j] = pp[j];
-    for (unsigned b = 1; b < gridDim.x; ++b) {
-      const volatile double* q = pp + (size_t)b * kMeasVals;
-      r[0] += q[0];
-      r[1] = fmax(r[1], q[1]);
-      for (int j = 2; j < 8; j += 2) { r[j] = fmin(r[j], q[j]); r[j + 1] = fmax(r[j + 1], q[j + 1]); }
-      r[8] += q[8];
-      r[9] += q[9];
-      r[10] = fmax(r[10], q[10]);
-    }
+  if (!s_last) return;
+  __threadfence();
+  // last block: every thread merges a strided subset of the block partials,
+  // then warps and finally thread 0 merge (a fixed, deterministic order)
+  double r[kMeasVals] = {0.0, -1e300, 1e300, -1e300, 1e300, -1e300, 1e300, -1e300, 0.0, 0.0, 0.0};
+  const volatile double* pp = partials;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock) {
+    double q[kMeasVals];
+    for (int j = 0; j < kMeasVals; ++j) q[j] = pp[(size_t)b * kMeasVals + j];
+    meas_merge(r, q);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double q[kMeasVals];
+#pragma unroll
+    for (int j = 0; j < kMeasVals; ++j) q[j] = __shfl_down_sync(0xffffffffu, r[j], o);
+    meas_merge(r, q);
+  }
+  __syncthreads();
+  if (lane == 0)
+    for (int j = 0; j < kMeasVals; ++j) sw[wid][j] = r[j];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kBlock / 32; ++w) meas_merge(r, sw[w]);
     const bool any = r[9] > 0.0;
     const double Dx = any ? r[3] - r[2] + 1.0 : 0.0;
     const double Dy = any ? r[5] - r[4] + 1.0 : 0.0;
@@ -681,17 +708,29 @@ __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, cons
 // Host-side launchers (called from lbm_capi.cu)
 // ---------------------------------------------------------------------------
 template <typename T>
-cudaError_t launch_step(const Consts<T>& k, const State<T>& s, bool raw, bool first, cudaStream_t st,
-                        cudaEvent_t mid) {
-  const int grid = (k.N + kBlock - 1) / kBlock;
-  if (raw) k_phi<T, true><<<grid, kBlock, 0, st>>>(k, s);
-  else k_phi<T, false><<<grid, kBlock, 0, st>>>(k, s);
-  if (mid) cudaEventRecord(mid, st);
-  if (raw && first) k_collide<T, true, true><<<grid, kBlock, 0, st>>>(k, s);
-  else if (raw) k_collide<T, true, false><<<grid, kBlock, 0, st>>>(k, s);
-  else if (first) k_collide<T, false, true><<<grid, kBlock, 0, st>>>(k, s);
-  else k_collide<T, false, false><<<grid, kBlock, 0, st>>>(k, s);
+size_t step_smem_bytes(const Tiling& tl) {
+  return (size_t)tl.hmax * (sizeof(T) + 1);
+}
+
+template <typename T, bool RAW, bool FIRST>
+static cudaError_t launch_step_t(const Consts<T>& k, const State<T>& s, const Tiling& tl, cudaStream_t st) {
+  const size_t sm = step_smem_bytes<T>(tl);
+  auto fn = k_step<T, RAW, FIRST>;
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<tl.ntx * tl.nty * tl.ntz, kBlock, sm, st>>>(k, s, tl);
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_step(const Consts<T>& k, const State<T>& s, const Tiling& tl, bool raw, bool first,
+                        cudaStream_t st) {
+  if (raw && first) return launch_step_t<T, true, true>(k, s, tl, st);
+  if (raw) return launch_step_t<T, true, false>(k, s, tl, st);
+  if (first) return launch_step_t<T, false, true>(k, s, tl, st);
+  return launch_step_t<T, false, false>(k, s, tl, st);
 }
 
 template <typename T, typename S>
@@ -728,8 +767,10 @@ cudaError_t launch_measure(int nx, int ny, int nz, const T* phi, const uint8_t* 
   return cudaGetLastError();
 }
 
-template cudaError_t launch_step<float>(const Consts<float>&, const State<float>&, bool, bool, cudaStream_t, cudaEvent_t);
-template cudaError_t launch_step<double>(const Consts<double>&, const State<double>&, bool, bool, cudaStream_t, cudaEvent_t);
+template size_t step_smem_bytes<float>(const Tiling&);
+template size_t step_smem_bytes<double>(const Tiling&);
+template cudaError_t launch_step<float>(const Consts<float>&, const State<float>&, const Tiling&, bool, bool, cudaStream_t);
+template cudaError_t launch_step<double>(const Consts<double>&, const State<double>&, const Tiling&, bool, bool, cudaStream_t);
 template cudaError_t launch_init<float, float>(const Consts<float>&, const State<float>&, const float*, const float*, cudaStream_t);
 template cudaError_t launch_init<float, double>(const Consts<float>&, const State<float>&, const double*, const double*, cudaStream_t);
 template cudaError_t launch_init<double, float>(const Consts<double>&, const State<double>&, const float*, const float*, cudaStream_t);
