@@ -217,6 +217,15 @@ def run_ours(args, rank, world, device):
     s.init_fields(C, u)
     for _ in range(W):
         s.step()
+    if args.tile:
+        s.set_tile(*[int(x) for x in args.tile.split(",")])
+        tile, tune_ms = tuple(int(x) for x in args.tile.split(",")), 0.0
+    elif not args.no_tune:
+        tile, tune_ms = s.autotune(reps=5)
+    else:
+        tile, tune_ms = (0, 0, 0), 0.0
+    for _ in range(2):
+        s.step()
     lib, h = s._lib, s._h
     stream = torch.cuda.current_stream(device)
     ms3 = (__import__("ctypes").c_float * 3)()
@@ -276,6 +285,7 @@ def run_ours(args, rank, world, device):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["label"], "nodes": n, "precision": "fp32 populations, fp32 math, "
                        "fp64 global sum", "parallelism": "replicas" if world > 1 else "single",
+                       "tile": list(tile), "tuned_ms": tune_ms,
                        "l2": "state (f, g: 732 MB) larger than L2 (129 MB): no flush"},
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
                     "d2h_bytes_per_step": d2h / K,
@@ -322,6 +332,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--tile", default=None, help="fixed tile 'tx,ty,tz' of the step kernel (no autotune)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -123,6 +123,13 @@ int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3)
 int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz);
 int lbm_get_tile(LbmHandle* h, int* txyz3);
 
+/* Tile autotuner: times `reps` launches of the next step kernel for each
+ * candidate tile shape on the handle's current state (which it leaves
+ * unchanged) and keeps the fastest.  Synchronises `stream`; allocates a
+ * temporary copy of u.  Outputs (may be NULL): the chosen extents and its
+ * time per launch in ms.  No reference counterpart. */
+int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* best_ms);
+
 /* Write the fields the reference exposes after the last step (or after
  * init) into caller device buffers of the handle's precision.  `mask` selects
  * LBM_FIELD_* bits; unselected pointers may be NULL.  Mirrors the attributes

@@ -199,19 +199,11 @@ State<T> make_state(const LbmHandle& h, int in_buf, int phi_in) {
   return s;
 }
 
-// Tiling of the fused step: z extent near 48 (balanced over nz), x and y
-// extents giving ~2.3k nodes per tile.
-Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz) {
-  if (tz <= 0) {
-    const int ntz = (int)((nz + 47) / 48);
-    tz = (int)((nz + ntz - 1) / ntz);
-  }
-  if (tx <= 0 || ty <= 0) {
-    int side = (int)std::lround(std::sqrt(2304.0 / tz));
-    side = std::max(2, std::min(side, 16));
-    if (tx <= 0) tx = side;
-    if (ty <= 0) ty = side;
-  }
+// Shared memory the step kernel may use per block: a third of an SM for float
+// (three resident blocks), most of one for double.
+size_t smem_budget(int prec) { return prec == LBM_F32 ? 70 * 1024 : 200 * 1024; }
+
+Tiling tiling_of(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz) {
   Tiling t;
   tx = std::max(tx, 2);
   ty = std::max(ty, 2);
@@ -224,6 +216,22 @@ Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz) {
   t.ntz = (int)((nz + t.tz - 1) / t.tz);
   t.hmax = (t.tx + 2) * (t.ty + 2) * (t.tz + 2);
   return t;
+}
+
+size_t tiling_smem(const Tiling& t, int prec) {
+  return prec == LBM_F32 ? step_smem_bytes<float>(t) : step_smem_bytes<double>(t);
+}
+
+// Default tiling of the fused step: z extent balanced over nz near 28 and a
+// 6 x 6 x-y cross-section (the shape the autotuner picks on the 150x150x107
+// ridge case).  Explicit extents (> 0) are taken as given.
+Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz, int prec) {
+  (void)prec;
+  if (tz <= 0) {
+    const int ntz = (int)((nz + 27) / 28);
+    tz = (int)((nz + ntz - 1) / ntz);
+  }
+  return tiling_of(nx, ny, nz, tx > 0 ? tx : 6, ty > 0 ? ty : 6, tz);
 }
 
 void free_all(LbmHandle* h) {
@@ -263,6 +271,27 @@ int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr
 
 }  // namespace
 
+namespace {
+// Times `reps` launches of the step kernel that would run next, without
+// advancing the state: the same input buffers are read every time and the
+// in-place velocity is restored from `u_save` by the caller.
+template <typename T>
+int time_tiling(LbmHandle* h, const Tiling& t, int reps, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
+                float* ms) {
+  const Consts<T>& k = consts_of<T>(*h);
+  State<T> s = make_state<T>(*h, h->cur, h->pc);
+  s.c_prev = h->c_last;
+  s.c_cur = h->c_last ^ 1;
+  CUDA_TRY(launch_step<T>(k, s, t, h->raw, h->first, st));  // warm-up (sets smem attribute)
+  CUDA_TRY(cudaEventRecord(e0, st));
+  for (int i = 0; i < reps; ++i) CUDA_TRY(launch_step<T>(k, s, t, h->raw, h->first, st));
+  CUDA_TRY(cudaEventRecord(e1, st));
+  CUDA_TRY(cudaEventSynchronize(e1));
+  CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+  return LBM_OK;
+}
+}  // namespace
+
 extern "C" {
 
 const char* lbm_last_error(void) { return g_err.c_str(); }
@@ -275,7 +304,7 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_create: 3-D grids with every extent >= 2 only");
   if (precision != LBM_F32 && precision != LBM_F64) return fail(LBM_E_ARG, "lbm_create: precision must be LBM_F32 or LBM_F64");
   const int64_t N = nx * ny * nz;
-  if (N > (int64_t)0x7fffffff / 2) return fail(LBM_E_ARG, "lbm_create: grid too large (N must be < 2^30)");
+  if (N * Q > (int64_t)0x7fffffff) return fail(LBM_E_ARG, "lbm_create: grid too large (19 N must be < 2^31)");
   if (params->stab_mode < 0 || params->stab_mode > 2) return fail(LBM_E_ARG, "lbm_create: bad stab_mode");
   if (!(params->tau_g > 0.5) || !(params->tau_l > 0.5)) return fail(LBM_E_ARG, "lbm_create: tau_l, tau_g must exceed 0.5");
   if (!(params->xi > 0)) return fail(LBM_E_ARG, "lbm_create: xi must be positive");
@@ -291,7 +320,7 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   h->wetting = params->theta_eq != 90.0 && params->kappa > 0;
   cudaGetDevice(&h->device);
   const size_t T = h->tsize;
-  h->tiling = make_tiling(nx, ny, nz, 0, 0, 0);
+  h->tiling = make_tiling(nx, ny, nz, 0, 0, 0, precision);
   // per-block partial sums: init (one block per 256 nodes), step (one per
   // tile; tile extents are at least 2) and measure
   const int nblocks = (int)((N + kBlock - 1) / kBlock);
@@ -436,10 +465,66 @@ int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz) {
   if (!h) return fail(LBM_E_ARG, "lbm_set_tile: null handle");
   if (tx == 1 || ty == 1 || tz == 1 || tx < 0 || ty < 0 || tz < 0 || tx > 64 || ty > 64 || tz > 256)
     return fail(LBM_E_ARG, "lbm_set_tile: tile extents must be in [2, 64] x [2, 64] x [2, 256] (0 = automatic)");
-  Tiling t = make_tiling(h->nx, h->ny, h->nz, tx, ty, tz);
-  const size_t sm = h->prec == LBM_F32 ? step_smem_bytes<float>(t) : step_smem_bytes<double>(t);
-  if (sm > 200 * 1024) return fail(LBM_E_ARG, "lbm_set_tile: tile too large for shared memory");
+  Tiling t = make_tiling(h->nx, h->ny, h->nz, tx, ty, tz, h->prec);
+  if (tiling_smem(t, h->prec) > 220 * 1024) return fail(LBM_E_ARG, "lbm_set_tile: tile too large for shared memory");
   h->tiling = t;
+  return LBM_OK;
+}
+
+
+int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* best_ms) {
+  if (!h) return fail(LBM_E_ARG, "lbm_autotune: null handle");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_autotune: call lbm_init_fields first");
+  if (reps <= 0) reps = 5;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t ub = 3 * (size_t)h->N * h->tsize;
+  void* u_save = nullptr;
+  CUDA_TRY(cudaMalloc(&u_save, ub));
+  CUDA_TRY(cudaMemcpyAsync(u_save, h->u, ub, cudaMemcpyDeviceToDevice, st));
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  // candidate tiles: z extents balanced over nz near 32 / 48 / 64, square
+  // x-y cross-sections of 4..16 nodes, shared memory within a third of an SM
+  std::vector<Tiling> cands;
+  for (int zt : {24, 32, 48, 64}) {
+    const int ntz = (int)((h->nz + zt - 1) / zt);
+    const int tz = (int)((h->nz + ntz - 1) / ntz);
+    for (int sx : {4, 5, 6, 8, 10, 12}) for (int sy : {4, 5, 6, 8, 10, 12}) {
+      if (sy < sx - 2 || sy > sx + 2) continue;
+      Tiling t = tiling_of(h->nx, h->ny, h->nz, sx, sy, tz);
+      if (tiling_smem(t, h->prec) > smem_budget(h->prec)) continue;
+      bool dup = false;
+      for (const Tiling& c : cands) dup |= (c.tx == t.tx && c.ty == t.ty && c.tz == t.tz);
+      if (!dup) cands.push_back(t);
+    }
+  }
+  Tiling best = h->tiling;
+  float best_t = 1e30f;
+  int rc = LBM_OK;
+  for (const Tiling& t : cands) {
+    float ms = 0.f;
+    rc = h->prec == LBM_F32 ? time_tiling<float>(h, t, reps, st, e0, e1, &ms)
+                            : time_tiling<double>(h, t, reps, st, e0, e1, &ms);
+    if (rc != LBM_OK) break;
+    if (ms < best_t) {
+      best_t = ms;
+      best = t;
+    }
+  }
+  cudaMemcpyAsync(h->u, u_save, ub, cudaMemcpyDeviceToDevice, st);
+  cudaStreamSynchronize(st);
+  cudaFree(u_save);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != LBM_OK) return rc;
+  h->tiling = best;
+  if (best_txyz3) {
+    best_txyz3[0] = best.tx;
+    best_txyz3[1] = best.ty;
+    best_txyz3[2] = best.tz;
+  }
+  if (best_ms) *best_ms = best_t / reps;
   return LBM_OK;
 }
 

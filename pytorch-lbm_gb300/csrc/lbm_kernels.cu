@@ -41,6 +41,36 @@ __device__ __forceinline__ T ldg(const T* p) {
   return __ldg(p);
 }
 
+// L2 cache policies.  KEEP (evict_last) marks the populations that phase A of
+// the step kernel reads and phase B reads again; ONCE (evict_first) marks
+// data touched once per step (g, u, phi, every store), so that it does not
+// displace them.
+struct Pol {
+  unsigned long long keep, once;
+  __device__ __forceinline__ static Pol make() {
+    Pol p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p.keep));
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p.once));
+    return p;
+  }
+};
+__device__ __forceinline__ float ld_pol(const float* p, unsigned long long pol) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_pol(const double* p, unsigned long long pol) {
+  double v;
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_pol(float* p, float v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol));
+}
+__device__ __forceinline__ void st_pol(double* p, double v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(pol));
+}
+
 // Separately rounded multiply and add (never contracted into an FMA).  The
 // isotropic gradient is accumulated with these so that mirror-symmetric
 // neighbour pairs cancel to exactly zero, as in the reference: the
@@ -102,24 +132,32 @@ __device__ __forceinline__ bool last_block_total(double part, double* partials, 
 // ---------------------------------------------------------------------------
 // Population reconstruction (pull form -> reference state at step start)
 // ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T ld_sel(const T* p, unsigned long long pol) {
+  return pol ? ld_pol(p, pol) : ldg(p);
+}
+
 template <typename T, bool RAW, bool WITH_C>
 __device__ __forceinline__ void fetch_pop(T (&v)[Q], const T* __restrict__ F, int n, size_t N,
-                                          const Nbr& nb, uint8_t c, T eps, T corr) {
+                                          const Nbr& nb, uint8_t c, T eps, T corr,
+                                          unsigned long long pol = 0ull) {
+  // element offsets q N + m stay below 2^31 (checked when the grid is created)
+  const unsigned Nu = (unsigned)N, nu = (unsigned)n;
   if (RAW) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ldg(F + (size_t)q * N + n);
+    for (int q = 0; q < Q; ++q) v[q] = ld_sel(F + (q * Nu + nu), pol);
     return;
   }
   if (c & kSolid) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ldg(F + (size_t)opp(q) * N + n);
+    for (int q = 0; q < Q; ++q) v[q] = ld_sel(F + (opp(q) * Nu + nu), pol);
   } else {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ldg(F + (size_t)q * N + nb.at(n, -ex(q), -ey(q), -ez(q)));
+    for (int q = 0; q < Q; ++q) v[q] = ld_sel(F + (q * Nu + (unsigned)nb.at(n, -ex(q), -ey(q), -ez(q))), pol);
     if (c & kPartial) {
       const T one_m = T(1) - eps;
 #pragma unroll
-      for (int q = 0; q < Q; ++q) v[q] = one_m * v[q] + eps * ldg(F + (size_t)opp(q) * N + n);
+      for (int q = 0; q < Q; ++q) v[q] = one_m * v[q] + eps * ld_sel(F + (opp(q) * Nu + nu), pol);
     }
   }
   if (WITH_C) {
@@ -157,9 +195,9 @@ __device__ __forceinline__ T relax_scale(T target, T sum_f) {
 // f at node n as the reference holds it at the start of the step.
 template <typename T, bool RAW>
 __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const State<T>& s, int n, size_t N,
-                                        const Nbr& nb, uint8_t c, T eps) {
+                                        const Nbr& nb, uint8_t c, T eps, unsigned long long pol = 0ull) {
   const T corr = RAW ? T(1) : s.cbuf[s.c_prev];
-  fetch_pop<T, RAW, !RAW>(v, s.fin, n, N, nb, c, eps, corr);
+  fetch_pop<T, RAW, !RAW>(v, s.fin, n, N, nb, c, eps, corr, pol);
   if (!RAW && k.relax_on && (c & kTop)) {
     const T r = relax_target(k, ldg(s.phi_in + n), corr);
     if (r >= T(0)) {
@@ -238,7 +276,7 @@ __device__ __forceinline__ T edot(int q, T a0, T a1, T a2) {
 // ---------------------------------------------------------------------------
 template <typename T, bool RAW, bool FIRST>
 __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>& s, int n, const Nbr& nb,
-                                             uint8_t c, T phi, T gx, T gy, T gz, T lap) {
+                                             uint8_t c, T phi, T gx, T gy, T gz, T lap, const Pol& pol) {
   const size_t N = (size_t)k.N;
   const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
@@ -271,28 +309,36 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>&
   // 3. pressure from the hydrodynamic populations
   const T eps = (c & kPartial) ? s.eps[n] : T(0);
   T g[Q];
-  fetch_pop<T, RAW, false>(g, s.gin, n, N, nb, c, eps, T(1));
+  fetch_pop<T, RAW, false>(g, s.gin, n, N, nb, c, eps, T(1), pol.once);
   const T P = seqsum(g);
 
-  // 4. non-equilibrium stress with the new P and the old u (:409-413)
-  const T uo0 = s.u[n], uo1 = s.u[N + n], uo2 = s.u[2 * N + n];
+  // 4. non-equilibrium stress with the new P and the old u (:409-413):
+  // sum_q e_a e_b (g_q - g_eq_q) = Pi_ab - P cs2 delta_ab - u_a u_b, since the
+  // D3Q19 weights satisfy sum w e_a e_b = cs2 delta_ab and
+  // sum w e_a e_b e_c e_d = cs2^2 (delta_ab delta_cd + delta_ac delta_bd + delta_ad delta_bc).
+  const unsigned Nu = (unsigned)N, nu = (unsigned)n;
+  const T uo0 = ld_pol(s.u + nu, pol.once), uo1 = ld_pol(s.u + (Nu + nu), pol.once),
+          uo2 = ld_pol(s.u + (2 * Nu + nu), pol.once);
   T sxx, syy, szz, sxy, sxz, syz;
   {
-    const T b = ((uo0 * uo0 + uo1 * uo1) + uo2 * uo2) * k.inv_two_cs2;
     bool fxx = true, fyy = true, fzz = true, fxy = true, fxz = true, fyz = true;
     sxx = syy = szz = sxy = sxz = syz = T(0);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const T ec = edot(q, uo0, uo1, uo2) * k.inv_cs2;
-      const T sq = k.w[q] * ((ec + ec * ec * T(0.5)) - b);
-      const T gneq = g[q] - (P * k.w[q] + sq);
-      if (ex(q) != 0) { sxx = fxx ? gneq : sxx + gneq; fxx = false; }
-      if (ey(q) != 0) { syy = fyy ? gneq : syy + gneq; fyy = false; }
-      if (ez(q) != 0) { szz = fzz ? gneq : szz + gneq; fzz = false; }
-      if (ex(q) * ey(q) != 0) { const T t = ex(q) * ey(q) > 0 ? gneq : -gneq; sxy = fxy ? t : sxy + t; fxy = false; }
-      if (ex(q) * ez(q) != 0) { const T t = ex(q) * ez(q) > 0 ? gneq : -gneq; sxz = fxz ? t : sxz + t; fxz = false; }
-      if (ey(q) * ez(q) != 0) { const T t = ey(q) * ez(q) > 0 ? gneq : -gneq; syz = fyz ? t : syz + t; fyz = false; }
+    for (int q = 1; q < Q; ++q) {
+      if (ex(q) != 0) { sxx = fxx ? g[q] : sxx + g[q]; fxx = false; }
+      if (ey(q) != 0) { syy = fyy ? g[q] : syy + g[q]; fyy = false; }
+      if (ez(q) != 0) { szz = fzz ? g[q] : szz + g[q]; fzz = false; }
+      if (ex(q) * ey(q) != 0) { const T t = ex(q) * ey(q) > 0 ? g[q] : -g[q]; sxy = fxy ? t : sxy + t; fxy = false; }
+      if (ex(q) * ez(q) != 0) { const T t = ex(q) * ez(q) > 0 ? g[q] : -g[q]; sxz = fxz ? t : sxz + t; fxz = false; }
+      if (ey(q) * ez(q) != 0) { const T t = ey(q) * ez(q) > 0 ? g[q] : -g[q]; syz = fyz ? t : syz + t; fyz = false; }
     }
+    const T pc = P * k.cs2;
+    sxx = (sxx - pc) - uo0 * uo0;
+    syy = (syy - pc) - uo1 * uo1;
+    szz = (szz - pc) - uo2 * uo2;
+    sxy = sxy - uo0 * uo1;
+    sxz = sxz - uo0 * uo2;
+    syz = syz - uo1 * uo2;
   }
 
   // 5. forces (Fakhari 2017, :416-439)
@@ -331,40 +377,10 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>&
     u2 = u2 + F2 * hr;
     if (c & kSolid) u0 = u1 = u2 = T(0);
   }
-
-  // 7. Allen-Cahn source (:450-494)
-  T S0, S1, S2;
-  {
-    T d0 = T(0), d1 = T(0), d2 = T(0);
-    if (!FIRST) {
-      const T pp = s.phi_in[n];
-      d0 = phi * u0 - pp * uo0;
-      d1 = phi * u1 - pp * uo1;
-      d2 = phi * u2 - pp * uo2;
-    }
-    T gm = sqrt((gx * gx + gy * gy) + gz * gz);
-    gm = gm < T(1e-10) ? T(1e-10) : gm;
-    const T lam = ((T(4) * phi) * (T(1) - phi)) * k.inv_W;
-    T cl = k.cs2 * lam * k.ac_scale * rcp(gm);
-    if (k.wetting) cl = cl * (T(1) - k.sharpen_reduce * k.ww[c >> kWwShift]);
-    S0 = d0 + cl * gx;
-    S1 = d1 + cl * gy;
-    S2 = d2 + cl * gz;
-  }
-
-  // 8. collisions (:496-530)
   const T b = ((u0 * u0 + u1 * u1) + u2 * u2) * k.inv_two_cs2;
-  {
-    T f[Q];
-    fetch_f<T, RAW>(f, k, s, n, N, nb, c, eps);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
-      const T feq = phi * (k.w[q] * (((T(1) + ec) + ec * ec * T(0.5)) - b));
-      const T src = k.wac3[q] * edot(q, S0, S1, S2);
-      s.fout[(size_t)q * N + n] = (f[q] - k.omega_f * (f[q] - feq)) + src;
-    }
-  }
+
+  // 8b. hydrodynamic collision (:503-530), before the phase-field one so that
+  // the 19 g values are dead before the 19 f values are loaded
   {
     T om;
     if (k.tau_const) {
@@ -380,24 +396,66 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>&
       const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
       const T geq = P * k.w[q] + k.w[q] * ((ec + ec * ec * T(0.5)) - b);
       const T G = (nsd * k.w[q]) * edot(q, F0, F1, F2);
-      s.gout[(size_t)q * N + n] = (g[q] - om * (g[q] - geq)) + G;
+      st_pol(s.gout + (q * Nu + nu), (g[q] - om * (g[q] - geq)) + G, pol.once);
     }
   }
-  s.u[n] = u0;
-  s.u[N + n] = u1;
-  s.u[2 * N + n] = u2;
-  s.phi_out[n] = phi;
+
+  // 7. Allen-Cahn source (:450-494)
+  T S0, S1, S2;
+  {
+    T d0 = T(0), d1 = T(0), d2 = T(0);
+    if (!FIRST) {
+      const T pp = ld_pol(s.phi_in + n, pol.once);
+      d0 = phi * u0 - pp * uo0;
+      d1 = phi * u1 - pp * uo1;
+      d2 = phi * u2 - pp * uo2;
+    }
+    T gm = sqrt((gx * gx + gy * gy) + gz * gz);
+    gm = gm < T(1e-10) ? T(1e-10) : gm;
+    const T lam = ((T(4) * phi) * (T(1) - phi)) * k.inv_W;
+    T cl = k.cs2 * lam * k.ac_scale * rcp(gm);
+    if (k.wetting) cl = cl * (T(1) - k.sharpen_reduce * k.ww[c >> kWwShift]);
+    S0 = d0 + cl * gx;
+    S1 = d1 + cl * gy;
+    S2 = d2 + cl * gz;
+  }
+
+  // 8a. phase-field collision (:496-500)
+  {
+    T f[Q];
+    fetch_f<T, RAW>(f, k, s, n, N, nb, c, eps);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
+      const T feq = phi * (k.w[q] * (((T(1) + ec) + ec * ec * T(0.5)) - b));
+      const T src = k.wac3[q] * edot(q, S0, S1, S2);
+      st_pol(s.fout + (q * Nu + nu), (f[q] - k.omega_f * (f[q] - feq)) + src, pol.once);
+    }
+  }
+  st_pol(s.u + nu, u0, pol.once);
+  st_pol(s.u + (Nu + nu), u1, pol.once);
+  st_pol(s.u + (2 * Nu + nu), u2, pol.once);
+  st_pol(s.phi_out + nu, phi, pol.once);
 }
 
 // ---------------------------------------------------------------------------
 // The fused time step
 // ---------------------------------------------------------------------------
+// Resident blocks per SM the step kernel is compiled for: three for float
+// (80 registers, no spills), one for double (no spills at double width).
+template <typename T>
+struct StepOccupancy {
+  static constexpr int blocks = sizeof(T) == 4 ? 3 : 1;
+};
+
 template <typename T, bool RAW, bool FIRST>
-__global__ void __launch_bounds__(kBlock) k_step(Consts<T> k, State<T> s, Tiling tl) {
+__global__ void __launch_bounds__(kBlock, StepOccupancy<T>::blocks) k_step(Consts<T> k, State<T> s, Tiling tl) {
+  // shared memory: phi and node class of the tile and its halo
   extern __shared__ __align__(16) unsigned char smem[];
   T* sphi = reinterpret_cast<T*>(smem);
   uint8_t* scls = reinterpret_cast<uint8_t*>(sphi + tl.hmax);
   const size_t N = (size_t)k.N;
+  const Pol pol = Pol::make();
 
   // tile of this CTA, clipped at the domain edge
   const int b = blockIdx.x;
@@ -407,32 +465,65 @@ __global__ void __launch_bounds__(kBlock) k_step(Consts<T> k, State<T> s, Tiling
   const int ex_ = min(tl.tx, k.nx - x0), ey_ = min(tl.ty, k.ny - y0), ez_ = min(tl.tz, k.nz - z0);
   const int HY = ey_ + 2, HZ = ez_ + 2;
   const int H = (ex_ + 2) * HY * HZ;
+  const int E = ex_ * ey_ * ez_;
   const float inv_hz = 1.0f / (float)HZ, inv_hy = 1.0f / (float)HY;
 
-  // phase A: phi on the tile and its halo
+  // phase A: phi on the tile and its halo; the tile's sum of phi accumulates in
+  // float64 so that it does not depend on the tiling
   double part = 0.0;
-  for (int h = threadIdx.x; h < H; h += kBlock) {
-    const int r = fdiv(h, inv_hz);
-    const int hz = h - r * HZ;
-    const int hx = fdiv(r, inv_hy);
-    const int hy = r - hx * HY;
-    int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
-    gx = gx < 0 ? gx + k.nx : (gx >= k.nx ? gx - k.nx : gx);
-    gy = gy < 0 ? gy + k.ny : (gy >= k.ny ? gy - k.ny : gy);
-    gz = gz < 0 ? gz + k.nz : (gz >= k.nz ? gz - k.nz : gz);
-    const int n = (gx * k.ny + gy) * k.nz + gz;
-    const uint8_t c = s.cls[n];
-    T phi = T(0);
-    if (!(c & kSolid)) {
-      const Nbr nb = make_nbr_xyz(gx, gy, gz, k.nx, k.ny, k.nz);
-      const T eps = (c & kPartial) ? s.eps[n] : T(0);
-      T v[Q];
-      fetch_f<T, RAW>(v, k, s, n, N, nb, c, eps);
-      phi = clamp01(seqsum(v));
+  // no periodic wrap anywhere in the halo or its pull sources: constant offsets
+  const bool inner = x0 >= 2 && x0 + ex_ + 2 <= k.nx && y0 >= 2 && y0 + ey_ + 2 <= k.ny && z0 >= 2 &&
+                     z0 + ez_ + 2 <= k.nz;
+  if (inner) {
+    Nbr nbc;
+    nbc.ox[0] = -k.ny * k.nz; nbc.ox[1] = 0; nbc.ox[2] = k.ny * k.nz;
+    nbc.oy[0] = -k.nz; nbc.oy[1] = 0; nbc.oy[2] = k.nz;
+    nbc.oz[0] = -1; nbc.oz[1] = 0; nbc.oz[2] = 1;
+    const int n00 = ((x0 - 1) * k.ny + (y0 - 1)) * k.nz + (z0 - 1);
+    for (int h = threadIdx.x; h < H; h += kBlock) {
+      const int r = fdiv(h, inv_hz);
+      const int hz = h - r * HZ;
+      const int hx = fdiv(r, inv_hy);
+      const int hy = r - hx * HY;
+      const int n = n00 + (hx * k.ny + hy) * k.nz + hz;
+      const uint8_t c = s.cls[n];
+      const bool own = hx >= 1 && hx <= ex_ && hy >= 1 && hy <= ey_ && hz >= 1 && hz <= ez_;
+      T phi = T(0);
+      if (!(c & kSolid)) {
+        const T eps = (c & kPartial) ? s.eps[n] : T(0);
+        T v[Q];
+        fetch_f<T, RAW>(v, k, s, n, N, nbc, c, eps, pol.keep);
+        phi = clamp01(seqsum(v));
+      }
+      sphi[h] = phi;
+      scls[h] = c;
+      if (own) part += (double)phi;
     }
-    sphi[h] = phi;
-    scls[h] = c;
-    if (hx >= 1 && hx <= ex_ && hy >= 1 && hy <= ey_ && hz >= 1 && hz <= ez_) part += (double)phi;
+  } else {
+    for (int h = threadIdx.x; h < H; h += kBlock) {
+      const int r = fdiv(h, inv_hz);
+      const int hz = h - r * HZ;
+      const int hx = fdiv(r, inv_hy);
+      const int hy = r - hx * HY;
+      int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
+      gx = gx < 0 ? gx + k.nx : (gx >= k.nx ? gx - k.nx : gx);
+      gy = gy < 0 ? gy + k.ny : (gy >= k.ny ? gy - k.ny : gy);
+      gz = gz < 0 ? gz + k.nz : (gz >= k.nz ? gz - k.nz : gz);
+      const int n = (gx * k.ny + gy) * k.nz + gz;
+      const uint8_t c = s.cls[n];
+      const bool own = hx >= 1 && hx <= ex_ && hy >= 1 && hy <= ey_ && hz >= 1 && hz <= ez_;
+      T phi = T(0);
+      if (!(c & kSolid)) {
+        const Nbr nb = make_nbr_xyz(gx, gy, gz, k.nx, k.ny, k.nz);
+        const T eps = (c & kPartial) ? s.eps[n] : T(0);
+        T v[Q];
+        fetch_f<T, RAW>(v, k, s, n, N, nb, c, eps, pol.keep);
+        phi = clamp01(seqsum(v));
+      }
+      sphi[h] = phi;
+      scls[h] = c;
+      if (own) part += (double)phi;
+    }
   }
   __syncthreads();
 
@@ -454,7 +545,6 @@ __global__ void __launch_bounds__(kBlock) k_step(Consts<T> k, State<T> s, Tiling
   }
 
   // phase B: the tile's nodes
-  const int E = ex_ * ey_ * ez_;
   const float inv_ez = 1.0f / (float)ez_, inv_ey = 1.0f / (float)ey_;
   const int sx = HY * HZ;
   for (int t = threadIdx.x; t < E; t += kBlock) {
@@ -474,7 +564,7 @@ __global__ void __launch_bounds__(kBlock) k_step(Consts<T> k, State<T> s, Tiling
                       [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; },
                       gx, gy, gz, lap);
     const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
-    collide_node<T, RAW, FIRST>(k, s, n, nb, c, phi, gx, gy, gz, lap);
+    collide_node<T, RAW, FIRST>(k, s, n, nb, c, phi, gx, gy, gz, lap, pol);
   }
 }
 
@@ -718,6 +808,8 @@ static cudaError_t launch_step_t(const Consts<T>& k, const State<T>& s, const Ti
   auto fn = k_step<T, RAW, FIRST>;
   if (sm > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
   }
   fn<<<tl.ntx * tl.nty * tl.ntz, kBlock, sm, st>>>(k, s, tl);

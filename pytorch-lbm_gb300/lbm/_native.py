@@ -23,7 +23,7 @@ EXPORTS = (
     "lbm_create", "lbm_destroy", "lbm_set_geometry", "lbm_init_fields", "lbm_step", "lbm_step_profiled",
     "lbm_get_fields", "lbm_get_populations", "lbm_get_geometry", "lbm_geometry_host",
     "lbm_get_scalars", "lbm_measure", "lbm_status", "lbm_last_error", "lbm_version",
-    "lbm_set_tile", "lbm_get_tile",
+    "lbm_set_tile", "lbm_get_tile", "lbm_autotune",
 )
 
 
@@ -65,6 +65,7 @@ def _declare(L):
         "lbm_status": ([_vp, ctypes.POINTER(_u32)], _i32),
         "lbm_set_tile": ([_vp, _i32, _i32, _i32], _i32),
         "lbm_get_tile": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),
+        "lbm_autotune": ([_vp, _i32, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)], _i32),
         "lbm_last_error": ([], ctypes.c_char_p),
         "lbm_version": ([], ctypes.c_char_p),
     }

@@ -363,6 +363,19 @@ class AllenCahnSolver:
         d["has_nan"] = bool(d["has_nan"])
         return d
 
+    def autotune(self, reps=5, stream=None):
+        """Pick the fastest tile shape of the step kernel on the current state
+        (the state is left unchanged).  Returns ((tx, ty, tz), ms per step)."""
+        t = (ctypes.c_int * 3)()
+        ms = ctypes.c_float()
+        nat.check(self._lib.lbm_autotune(self._h, int(reps), nat.stream_ptr(stream), t, ctypes.byref(ms)),
+                  "lbm_autotune")
+        return (t[0], t[1], t[2]), float(ms.value)
+
+    def set_tile(self, tx, ty, tz):
+        """Tile extents of the step kernel (0 = automatic)."""
+        nat.check(self._lib.lbm_set_tile(self._h, int(tx), int(ty), int(tz)), "lbm_set_tile")
+
     def status(self):
         v = ctypes.c_uint32()
         nat.check(self._lib.lbm_status(self._h, ctypes.byref(v)), "lbm_status")
