@@ -46,6 +46,9 @@ import numpy as np  # noqa: E402
 B_ALG_STEP = 336
 # The fused step kernel k_step moves those 336 B plus the node-class byte.
 B_ALG_KERNEL = 337
+# Half-precision population storage: 2 x 2 x 38 + 2 x 4 x 4 = 184 B (+1).
+B_ALG_STEP_F16 = 184
+B_ALG_KERNEL_F16 = 185
 
 WORKLOADS = {
     "ridge150": dict(grid=(150, 150, 107), substrate=("ridge", 1.0, 22.5), center=(75, 75, 80),
@@ -212,7 +215,8 @@ def run_ours(args, rank, world, device):
     K, W = args.steps, args.warmup
 
     # --- device-resident timed region -------------------------------------
-    s = AllenCahnSolver(cfg, dtype=torch.float32, geo_amplification=1.5, geometric_wetting=True)
+    pdt = torch.float16 if args.precision == "fp16" else torch.float32
+    s = AllenCahnSolver(cfg, dtype=pdt, geo_amplification=1.5, geometric_wetting=True)
     s.set_solid(solid, frac)
     s.init_fields(C, u)
     for _ in range(W):
@@ -248,7 +252,7 @@ def run_ours(args, rank, world, device):
     torch.cuda.synchronize(device)
     barrier(world)
     t0 = time.perf_counter()
-    s2 = AllenCahnSolver(cfg, dtype=torch.float32, geo_amplification=1.5, geometric_wetting=True)
+    s2 = AllenCahnSolver(cfg, dtype=pdt, geo_amplification=1.5, geometric_wetting=True)
     s2.set_solid(solid, frac)
     s2.init_fields(C, u)
     reads = 0
@@ -268,10 +272,13 @@ def run_ours(args, rank, world, device):
     out = None
     if rank == 0:
         peak, peak_kind = peaks()
+        f16 = args.precision == "fp16"
+        b_ker = B_ALG_KERNEL_F16 if f16 else B_ALG_KERNEL
+        b_step = B_ALG_STEP_F16 if f16 else B_ALG_STEP
         ker_s = ker_ms / K / 1e3
-        achieved = B_ALG_KERNEL * n / ker_s / 1e9
-        traffic_pn = profiled_traffic("k_step")
-        step_bw = B_ALG_STEP * n / (tot_ms / K / 1e3) / 1e9
+        achieved = b_ker * n / ker_s / 1e9
+        traffic_pn = profiled_traffic("k_step_f16" if f16 else "k_step")
+        step_bw = b_step * n / (tot_ms / K / 1e3) / 1e9
         w = WORKLOADS[name]
         cpu = None
         if not args.no_cpu_baseline:
@@ -283,8 +290,10 @@ def run_ours(args, rank, world, device):
             "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": tot_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": w["label"], "nodes": n, "precision": "fp32 populations, fp32 math, "
-                       "fp64 global sum", "parallelism": "replicas" if world > 1 else "single",
+            "config": {"workload": w["label"], "nodes": n,
+                       "precision": ("fp16 deviation-stored populations, fp32 math and fields, fp64 global sum"
+                                     if f16 else "fp32 populations, fp32 math, fp64 global sum"),
+                       "parallelism": "replicas" if world > 1 else "single",
                        "tile": list(tile), "tuned_ms": tune_ms,
                        "l2": "state (f, g: 732 MB) larger than L2 (129 MB): no flush"},
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
@@ -294,10 +303,10 @@ def run_ours(args, rank, world, device):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic_pn * n if traffic_pn is not None else None,
-                         "kernel": "k_step", "bytes_per_node": B_ALG_KERNEL,
+                         "kernel": "k_step", "bytes_per_node": b_ker,
                          "ms_per_launch": ker_ms / K},
-            "step_roofline": {"achieved_gbs": step_bw, "bytes_per_node": B_ALG_STEP, "peak": peak,
-                              "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / B_ALG_STEP},
+            "step_roofline": {"achieved_gbs": step_bw, "bytes_per_node": b_step, "peak": peak,
+                              "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / b_step},
             "gpu_launches": K,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
@@ -333,6 +342,7 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--tile", default=None, help="fixed tile 'tx,ty,tz' of the step kernel (no autotune)")
     args = ap.parse_args()
     if args.warmup < 3:

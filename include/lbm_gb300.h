@@ -34,6 +34,10 @@ extern "C" {
 /* Precision of the state and of the collision arithmetic. */
 #define LBM_F32 0           /* float populations, float arithmetic            */
 #define LBM_F64 1           /* double populations, double arithmetic          */
+#define LBM_F16 2           /* half populations stored as deviations from the
+                               rest-state equilibria (f: F/w - phi of the
+                               reading node, g: G/w), float arithmetic and
+                               fields, double global sums                   */
 
 /* Element type of a caller array. */
 #define LBM_DT_NONE 0
@@ -131,7 +135,8 @@ int lbm_get_tile(LbmHandle* h, int* txyz3);
 int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* best_ms);
 
 /* Write the fields the reference exposes after the last step (or after
- * init) into caller device buffers of the handle's precision.  `mask` selects
+ * init) into caller device buffers of the handle's compute type (float for
+ * LBM_F32 and LBM_F16, double for LBM_F64).  `mask` selects
  * LBM_FIELD_* bits; unselected pointers may be NULL.  Mirrors the attributes
  * phi, rho, u, P, p, mu_phi of AllenCahnSolver (lbm/fe_ac_solver.py:97-116,
  * values as assigned in step()). */
@@ -139,7 +144,7 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u,
                    void* P, void* p, void* mu, void* stream);
 
 /* Current populations f, g (19N each, caller device buffers of the handle's
- * precision) as the reference holds them between steps (AllenCahnSolver.f/.g,
+ * compute type) as the reference holds them between steps (AllenCahnSolver.f/.g,
  * lbm/fe_ac_solver.py:97-98). */
 int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream);
 

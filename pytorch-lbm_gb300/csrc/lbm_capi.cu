@@ -1,5 +1,6 @@
 // C ABI of the GB300 Allen-Cahn phase-field LBM (declarations and the
 // reference interface each entry point replaces: include/lbm_gb300.h).
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,15 +19,15 @@
 namespace lbm {
 template <typename T>
 size_t step_smem_bytes(const Tiling&);
-template <typename T>
-cudaError_t launch_step(const Consts<T>&, const State<T>&, const Tiling&, bool, bool, cudaStream_t);
 template <typename T, typename S>
-cudaError_t launch_init(const Consts<T>&, const State<T>&, const S*, const S*, cudaStream_t);
-template <typename T>
-cudaError_t launch_observe(const Consts<T>&, const State<T>&, bool, unsigned, int, T*, T*, T*, T*, T*, T*,
+cudaError_t launch_step(const Consts<T>&, const State<T, S>&, const Tiling&, bool, bool, cudaStream_t);
+template <typename T, typename S, typename Src>
+cudaError_t launch_init(const Consts<T>&, const State<T, S>&, const Src*, const Src*, cudaStream_t);
+template <typename T, typename S>
+cudaError_t launch_observe(const Consts<T>&, const State<T, S>&, bool, unsigned, int, T*, T*, T*, T*, T*, T*,
                            cudaStream_t);
-template <typename T>
-cudaError_t launch_populations(const Consts<T>&, const State<T>&, bool, T*, T*, cudaStream_t);
+template <typename T, typename S>
+cudaError_t launch_populations(const Consts<T>&, const State<T, S>&, bool, T*, T*, cudaStream_t);
 template <typename T>
 cudaError_t launch_measure(int, int, int, const T*, const uint8_t*, double*, int, unsigned*, double*,
                            cudaStream_t);
@@ -56,7 +57,8 @@ struct LbmHandle {
   int prec = LBM_F32;
   int64_t nx = 0, ny = 0, nz = 0, N = 0;
   int device = 0;
-  size_t tsize = 4;
+  size_t tsize = 4;  // compute type (u, phi, eps, fields)
+  size_t psize = 4;  // population storage type
   // device memory
   void* f[2] = {nullptr, nullptr};
   void* g[2] = {nullptr, nullptr};
@@ -108,6 +110,7 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
     k.w2c[q] = (T)2 * k.wc[q];
     k.wac[q] = (T)ac_coeff * (T)wf;
     k.wac3[q] = k.wac[q] / (T)cs2;
+    k.inv_w[q] = (T)1 / (T)wf;
   }
   k.cs2 = (T)cs2;
   k.two_cs2 = (T)(2.0 * cs2);
@@ -176,15 +179,29 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   return k;
 }
 
+// Compute / storage type pair of a precision: float/float, double/double,
+// float/half (deviation-storage form).
+template <typename T_, typename S_>
+struct Types {
+  using T = T_;
+  using S = S_;
+};
+template <typename Fn>
+auto with_types(int prec, Fn&& fn) {
+  if (prec == LBM_F64) return fn(Types<double, double>{});
+  if (prec == LBM_F16) return fn(Types<float, __half>{});
+  return fn(Types<float, float>{});
+}
+
 // State of a step reading population buffer `in_buf` and phi buffer `phi_in`.
-template <typename T>
-State<T> make_state(const LbmHandle& h, int in_buf, int phi_in) {
-  State<T> s;
+template <typename T, typename S>
+State<T, S> make_state(const LbmHandle& h, int in_buf, int phi_in) {
+  State<T, S> s;
   std::memset(&s, 0, sizeof(s));
-  s.fin = static_cast<const T*>(h.f[in_buf]);
-  s.gin = static_cast<const T*>(h.g[in_buf]);
-  s.fout = static_cast<T*>(h.f[in_buf ^ 1]);
-  s.gout = static_cast<T*>(h.g[in_buf ^ 1]);
+  s.fin = static_cast<const S*>(h.f[in_buf]);
+  s.gin = static_cast<const S*>(h.g[in_buf]);
+  s.fout = static_cast<S*>(h.f[in_buf ^ 1]);
+  s.gout = static_cast<S*>(h.g[in_buf ^ 1]);
   s.u = static_cast<T*>(h.u);
   s.phi_in = static_cast<const T*>(h.phi[phi_in]);
   s.phi_out = static_cast<T*>(h.phi[phi_in ^ 1]);
@@ -201,7 +218,7 @@ State<T> make_state(const LbmHandle& h, int in_buf, int phi_in) {
 
 // Shared memory the step kernel may use per block: a third of an SM for float
 // (three resident blocks), most of one for double.
-size_t smem_budget(int prec) { return prec == LBM_F32 ? 70 * 1024 : 200 * 1024; }
+size_t smem_budget(int prec) { return prec == LBM_F64 ? 200 * 1024 : 70 * 1024; }
 
 Tiling tiling_of(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz) {
   Tiling t;
@@ -219,7 +236,7 @@ Tiling tiling_of(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz) {
 }
 
 size_t tiling_smem(const Tiling& t, int prec) {
-  return prec == LBM_F32 ? step_smem_bytes<float>(t) : step_smem_bytes<double>(t);
+  return prec == LBM_F64 ? step_smem_bytes<double>(t) : step_smem_bytes<float>(t);
 }
 
 // Default tiling of the fused step: z extent balanced over nz near 28 and a
@@ -248,11 +265,11 @@ const Consts<float>& consts_of<float>(const LbmHandle& h) { return h.kf; }
 template <>
 const Consts<double>& consts_of<double>(const LbmHandle& h) { return h.kd; }
 
-template <typename T>
+template <typename T, typename S>
 int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr) {
   const Consts<T>& k = consts_of<T>(*h);
   for (int i = 0; i < nsteps; ++i) {
-    State<T> s = make_state<T>(*h, h->cur, h->pc);
+    State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
     s.c_prev = h->c_last;
     s.c_cur = h->c_last ^ 1;
     if (ev) CUDA_TRY(cudaEventRecord(ev[i], st));
@@ -275,11 +292,11 @@ namespace {
 // Times `reps` launches of the step kernel that would run next, without
 // advancing the state: the same input buffers are read every time and the
 // in-place velocity is restored from `u_save` by the caller.
-template <typename T>
+template <typename T, typename S>
 int time_tiling(LbmHandle* h, const Tiling& t, int reps, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
                 float* ms) {
   const Consts<T>& k = consts_of<T>(*h);
-  State<T> s = make_state<T>(*h, h->cur, h->pc);
+  State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
   s.c_prev = h->c_last;
   s.c_cur = h->c_last ^ 1;
   CUDA_TRY(launch_step<T>(k, s, t, h->raw, h->first, st));  // warm-up (sets smem attribute)
@@ -302,7 +319,8 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   if (!params || !out) return fail(LBM_E_ARG, "lbm_create: null argument");
   *out = nullptr;
   if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_create: 3-D grids with every extent >= 2 only");
-  if (precision != LBM_F32 && precision != LBM_F64) return fail(LBM_E_ARG, "lbm_create: precision must be LBM_F32 or LBM_F64");
+  if (precision != LBM_F32 && precision != LBM_F64 && precision != LBM_F16)
+    return fail(LBM_E_ARG, "lbm_create: precision must be LBM_F32, LBM_F64 or LBM_F16");
   const int64_t N = nx * ny * nz;
   if (N * Q > (int64_t)0x7fffffff) return fail(LBM_E_ARG, "lbm_create: grid too large (19 N must be < 2^31)");
   if (params->stab_mode < 0 || params->stab_mode > 2) return fail(LBM_E_ARG, "lbm_create: bad stab_mode");
@@ -316,7 +334,8 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   h->ny = ny;
   h->nz = nz;
   h->N = N;
-  h->tsize = precision == LBM_F32 ? 4 : 8;
+  h->tsize = precision == LBM_F64 ? 8 : 4;
+  h->psize = precision == LBM_F64 ? 8 : (precision == LBM_F16 ? 2 : 4);
   h->wetting = params->theta_eq != 90.0 && params->kappa > 0;
   cudaGetDevice(&h->device);
   const size_t T = h->tsize;
@@ -331,8 +350,8 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
     if (e == cudaSuccess) e = cudaMalloc(p, bytes);
   };
   for (int b = 0; b < 2; ++b) {
-    A(&h->f[b], (size_t)Q * N * T);
-    A(&h->g[b], (size_t)Q * N * T);
+    A(&h->f[b], (size_t)Q * N * h->psize);
+    A(&h->g[b], (size_t)Q * N * h->psize);
   }
   A(&h->u, 3 * N * T);
   A(&h->phi[0], N * T);
@@ -371,7 +390,7 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
   const int64_t N = h->N;
   CUDA_TRY(cudaMemcpy(h->cls, h->geo.cls.data(), N, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(h->wn, h->geo.wall_normal.data(), 3 * N * sizeof(float), cudaMemcpyHostToDevice));
-  if (h->prec == LBM_F32) {
+  if (h->prec != LBM_F64) {
     std::vector<float> eps(N, 0.0f);
     if (!h->geo.fraction.empty())
       for (int64_t n = 0; n < N; ++n) eps[n] = (float)h->geo.fraction[n];
@@ -410,18 +429,14 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
       du = stage + N * es;
     }
   }
-  cudaError_t e;
-  if (h->prec == LBM_F32) {
-    State<float> s = make_state<float>(*h, in, h->pc ^ 1);
-    e = src_dtype == LBM_DT_F32
-            ? launch_init<float, float>(h->kf, s, (const float*)dphi, (const float*)du, st)
-            : launch_init<float, double>(h->kf, s, (const double*)dphi, (const double*)du, st);
-  } else {
-    State<double> s = make_state<double>(*h, in, h->pc ^ 1);
-    e = src_dtype == LBM_DT_F32
-            ? launch_init<double, float>(h->kd, s, (const float*)dphi, (const float*)du, st)
-            : launch_init<double, double>(h->kd, s, (const double*)dphi, (const double*)du, st);
-  }
+  cudaError_t e = with_types(h->prec, [&](auto tag) {
+    using T = typename decltype(tag)::T;
+    using S = typename decltype(tag)::S;
+    State<T, S> s = make_state<T, S>(*h, in, h->pc ^ 1);
+    return src_dtype == LBM_DT_F32
+               ? launch_init<T, S, float>(consts_of<T>(*h), s, (const float*)dphi, (const float*)du, st)
+               : launch_init<T, S, double>(consts_of<T>(*h), s, (const double*)dphi, (const double*)du, st);
+  });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_init_fields: ") + cudaGetErrorString(e));
   h->initialized = true;
   h->raw = true;
@@ -437,7 +452,9 @@ int lbm_step(LbmHandle* h, int nsteps, void* stream) {
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_step: call lbm_init_fields first");
   if (nsteps < 0) return fail(LBM_E_ARG, "lbm_step: negative step count");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  return h->prec == LBM_F32 ? do_step<float>(h, nsteps, st) : do_step<double>(h, nsteps, st);
+  return with_types(h->prec, [&](auto tag) {
+    return do_step<typename decltype(tag)::T, typename decltype(tag)::S>(h, nsteps, st);
+  });
 }
 
 int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3) {
@@ -447,7 +464,9 @@ int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3)
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   std::vector<cudaEvent_t> ev((size_t)nsteps + 1, nullptr);
   for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
-  int rc = h->prec == LBM_F32 ? do_step<float>(h, nsteps, st, ev.data()) : do_step<double>(h, nsteps, st, ev.data());
+  int rc = with_types(h->prec, [&](auto tag) {
+    return do_step<typename decltype(tag)::T, typename decltype(tag)::S>(h, nsteps, st, ev.data());
+  });
   float tot = 0.f;
   if (rc == LBM_OK) {
     cudaError_t e = cudaEventSynchronize(ev.back());
@@ -504,8 +523,9 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
   int rc = LBM_OK;
   for (const Tiling& t : cands) {
     float ms = 0.f;
-    rc = h->prec == LBM_F32 ? time_tiling<float>(h, t, reps, st, e0, e1, &ms)
-                            : time_tiling<double>(h, t, reps, st, e0, e1, &ms);
+    rc = with_types(h->prec, [&](auto tag) {
+      return time_tiling<typename decltype(tag)::T, typename decltype(tag)::S>(h, t, reps, st, e0, e1, &ms);
+    });
     if (rc != LBM_OK) break;
     if (ms < best_t) {
       best_t = ms;
@@ -548,17 +568,14 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u, v
   const int in_buf = h->steps == 0 ? h->cur : (h->cur ^ 1);  // the last step's input buffer
   cudaError_t e;
   // phi_out of the state = the latest recovered phi
-  if (h->prec == LBM_F32) {
-    State<float> s = make_state<float>(*h, in_buf, h->pc ^ 1);
+  e = with_types(h->prec, [&](auto tag) {
+    using T = typename decltype(tag)::T;
+    using S = typename decltype(tag)::S;
+    State<T, S> s = make_state<T, S>(*h, in_buf, h->pc ^ 1);
     s.c_cur = h->c_last;
-    e = launch_observe<float>(h->kf, s, h->last_raw_in, mask, mode, (float*)phi, (float*)rho, (float*)u,
-                              (float*)P, (float*)p, (float*)mu, st);
-  } else {
-    State<double> s = make_state<double>(*h, in_buf, h->pc ^ 1);
-    s.c_cur = h->c_last;
-    e = launch_observe<double>(h->kd, s, h->last_raw_in, mask, mode, (double*)phi, (double*)rho, (double*)u,
-                               (double*)P, (double*)p, (double*)mu, st);
-  }
+    return launch_observe<T, S>(consts_of<T>(*h), s, h->last_raw_in, mask, mode, (T*)phi, (T*)rho, (T*)u,
+                                (T*)P, (T*)p, (T*)mu, st);
+  });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_get_fields: ") + cudaGetErrorString(e));
   return LBM_OK;
 }
@@ -569,15 +586,13 @@ int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
   // fin = the current state, phi_in = the latest phi, c_prev = its correction
-  if (h->prec == LBM_F32) {
-    State<float> s = make_state<float>(*h, h->cur, h->pc);
+  e = with_types(h->prec, [&](auto tag) {
+    using T = typename decltype(tag)::T;
+    using S = typename decltype(tag)::S;
+    State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
     s.c_prev = h->c_last;
-    e = launch_populations<float>(h->kf, s, h->raw, (float*)f, (float*)g, st);
-  } else {
-    State<double> s = make_state<double>(*h, h->cur, h->pc);
-    s.c_prev = h->c_last;
-    e = launch_populations<double>(h->kd, s, h->raw, (double*)f, (double*)g, st);
-  }
+    return launch_populations<T, S>(consts_of<T>(*h), s, h->raw, (T*)f, (T*)g, st);
+  });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_get_populations: ") + cudaGetErrorString(e));
   return LBM_OK;
 }
@@ -627,7 +642,7 @@ int lbm_get_scalars(LbmHandle* h, double* phi_mass_init, double* last_sum_phi, d
   if (last_correction) {
     double c = 1.0;
     if (h->initialized && h->steps > 0) {
-      if (h->prec == LBM_F32) {
+      if (h->prec != LBM_F64) {
         float v;
         CUDA_TRY(cudaMemcpy(&v, static_cast<float*>(h->cbuf) + h->c_last, sizeof(float), cudaMemcpyDeviceToHost));
         c = v;
@@ -648,7 +663,7 @@ int lbm_measure(LbmHandle* h, double* out9, void* stream) {
   int rc = lbm_get_fields(h, LBM_FIELD_PHI, h->meas_phi, nullptr, nullptr, nullptr, nullptr, nullptr, stream);
   if (rc) return rc;
   cudaError_t e;
-  if (h->prec == LBM_F32)
+  if (h->prec != LBM_F64)
     e = launch_measure<float>((int)h->nx, (int)h->ny, (int)h->nz, (const float*)h->meas_phi, h->cls, h->partials,
                               kMeasureBlocks, h->counters + 1, h->scal + 2, st);
   else

@@ -99,6 +99,7 @@ struct Consts {
   T w2c[Q];    // 2 w_i / cs2                    (laplacian weights)
   T wac[Q];    // (1 - 1/(2 tau_f)) w_i          (Allen-Cahn source)
   T wac3[Q];   // wac_i / cs2
+  T inv_w[Q];  // 1 / w_i (deviation storage)
   T cs2, two_cs2, inv_cs2, inv_two_cs2, inv_W;
   T beta4, kappa, phi_c, W;
   T rho_l, rho_g, rho_floor, drho;
@@ -120,13 +121,14 @@ struct Consts {
   T ww[16];              // near-wall weight by code (float32 values)
 };
 
-// Device state of one grid.
-template <typename T>
+// Device state of one grid.  T is the compute type, S the population
+// storage type (T itself, or half for the deviation-storage form).
+template <typename T, typename S = T>
 struct State {
-  const T* fin;   // populations read this step (post-collision of the last step, or raw)
-  const T* gin;
-  T* fout;        // post-collision populations written this step
-  T* gout;
+  const S* fin;   // populations read this step (post-collision of the last step, or raw)
+  const S* gin;
+  S* fout;        // post-collision populations written this step
+  S* gout;
   T* u;           // velocity [3][N], in place
   const T* phi_in;  // phi recovered by the last step (before its mass correction)
   T* phi_out;       // phi recovered by this step

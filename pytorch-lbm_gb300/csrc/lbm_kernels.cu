@@ -24,6 +24,7 @@
 // deterministic last-block reduction of the per-tile partial sums.
 // Arithmetic follows the reference's operation order; sums run in population
 // order; the isotropic gradient is accumulated without FMA contraction.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "lbm_common.cuh"
@@ -46,11 +47,12 @@ __device__ __forceinline__ T ldg(const T* p) {
 // data touched once per step (g, u, phi, every store), so that it does not
 // displace them.
 struct Pol {
-  unsigned long long keep, once;
+  unsigned long long keep, once, same;
   __device__ __forceinline__ static Pol make() {
     Pol p;
     asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p.keep));
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p.once));
+    asm("createpolicy.fractional.L2::evict_unchanged.b64 %0, 1.0;" : "=l"(p.same));
     return p;
   }
 };
@@ -70,6 +72,45 @@ __device__ __forceinline__ void st_pol(float* p, float v, unsigned long long pol
 __device__ __forceinline__ void st_pol(double* p, double v, unsigned long long pol) {
   asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(pol));
 }
+__device__ __forceinline__ __half ld_pol(const __half* p, unsigned long long pol) {
+  unsigned short v;
+  asm("ld.global.nc.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return __ushort_as_half(v);
+}
+__device__ __forceinline__ void st_pol(__half* p, __half v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.b16 [%0], %1, %2;" ::"l"(p), "h"(__half_as_ushort(v)), "l"(pol));
+}
+
+// Population storage.  S == T stores the population itself.  S == half (the
+// deviation-storage form) stores f as its normalised deviation from the
+// rest-state equilibrium w_q phi, d = F / w_q - phi_ref, where phi_ref is the
+// phi of the node that will read the value (its own phi of the previous step,
+// known to the reader without a load), and g as G / w_q (its rest-state
+// equilibrium w_q P has P ~ 0).  Arithmetic is always in T.
+template <typename T, typename S>
+struct PopIO {
+  static constexpr bool kDev = false;
+  __device__ __forceinline__ static T ld_f(S raw, int, T, const Consts<T>&) { return raw; }
+  __device__ __forceinline__ static S st_f(T v, int, T, const Consts<T>&) { return v; }
+  __device__ __forceinline__ static T ld_g(S raw, int, const Consts<T>&) { return raw; }
+  __device__ __forceinline__ static S st_g(T v, int, const Consts<T>&) { return v; }
+};
+template <>
+struct PopIO<float, __half> {
+  static constexpr bool kDev = true;
+  __device__ __forceinline__ static float ld_f(__half raw, int q, float ref, const Consts<float>& k) {
+    return k.w[q] * (__half2float(raw) + ref);
+  }
+  __device__ __forceinline__ static __half st_f(float v, int q, float ref, const Consts<float>& k) {
+    return __float2half_rn(v * k.inv_w[q] - ref);
+  }
+  __device__ __forceinline__ static float ld_g(__half raw, int q, const Consts<float>& k) {
+    return k.w[q] * __half2float(raw);
+  }
+  __device__ __forceinline__ static __half st_g(float v, int q, const Consts<float>& k) {
+    return __float2half_rn(v * k.inv_w[q]);
+  }
+};
 
 // Separately rounded multiply and add (never contracted into an FMA).  The
 // isotropic gradient is accumulated with these so that mirror-symmetric
@@ -132,32 +173,50 @@ __device__ __forceinline__ bool last_block_total(double part, double* partials, 
 // ---------------------------------------------------------------------------
 // Population reconstruction (pull form -> reference state at step start)
 // ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ T ld_sel(const T* p, unsigned long long pol) {
-  return pol ? ld_pol(p, pol) : ldg(p);
+// Loads of the step kernel carry an L2 policy; the read-out kernels (no
+// policy) use plain read-only loads.
+template <bool USE_POL, typename S>
+__device__ __forceinline__ S ld_sel(const S* p, unsigned long long pol) {
+  if constexpr (USE_POL) return ld_pol(p, pol);
+  else return ldg(p);
 }
+__device__ __forceinline__ __half ldg(const __half* p) { return __ldg(p); }
 
-template <typename T, bool RAW, bool WITH_C>
-__device__ __forceinline__ void fetch_pop(T (&v)[Q], const T* __restrict__ F, int n, size_t N,
-                                          const Nbr& nb, uint8_t c, T eps, T corr,
-                                          unsigned long long pol = 0ull) {
+// Populations of node n as the reference holds them at the start of the step
+// (before the mass correction, which WITH_C applies).  IS_F selects the
+// f encoding of PopIO; phi_in (the previous step's phi) supplies the deviation
+// references of the half form: the node's own phi for pulled values, the
+// neighbour x - e_q's phi for the node's own opposite slot (bounce-back, VP).
+template <typename T, typename S, bool RAW, bool WITH_C, bool IS_F, bool USE_POL = false>
+__device__ __forceinline__ void fetch_pop(T (&v)[Q], const Consts<T>& k, const S* __restrict__ F,
+                                          const T* __restrict__ phi_in, int n, size_t N, const Nbr& nb,
+                                          uint8_t c, T eps, T corr, unsigned long long pol = 0ull) {
+  using IO = PopIO<T, S>;
   // element offsets q N + m stay below 2^31 (checked when the grid is created)
   const unsigned Nu = (unsigned)N, nu = (unsigned)n;
+  const T ref_self = (IO::kDev && IS_F) ? ldg(phi_in + n) : T(0);
+  auto ld = [&](int q, unsigned idx, T ref) -> T {
+    const S raw = ld_sel<USE_POL>(F + idx, pol);
+    return IS_F ? IO::ld_f(raw, q, ref, k) : IO::ld_g(raw, q, k);
+  };
+  auto ref_nb = [&](int q) -> T {
+    return (IO::kDev && IS_F) ? ldg(phi_in + nb.at(n, -ex(q), -ey(q), -ez(q))) : T(0);
+  };
   if (RAW) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ld_sel(F + (q * Nu + nu), pol);
+    for (int q = 0; q < Q; ++q) v[q] = ld(q, q * Nu + nu, ref_self);
     return;
   }
   if (c & kSolid) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ld_sel(F + (opp(q) * Nu + nu), pol);
+    for (int q = 0; q < Q; ++q) v[q] = ld(opp(q), opp(q) * Nu + nu, ref_nb(q));
   } else {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ld_sel(F + (q * Nu + (unsigned)nb.at(n, -ex(q), -ey(q), -ez(q))), pol);
+    for (int q = 0; q < Q; ++q) v[q] = ld(q, q * Nu + (unsigned)nb.at(n, -ex(q), -ey(q), -ez(q)), ref_self);
     if (c & kPartial) {
       const T one_m = T(1) - eps;
 #pragma unroll
-      for (int q = 0; q < Q; ++q) v[q] = one_m * v[q] + eps * ld_sel(F + (opp(q) * Nu + nu), pol);
+      for (int q = 0; q < Q; ++q) v[q] = one_m * v[q] + eps * ld(opp(q), opp(q) * Nu + nu, ref_nb(q));
     }
   }
   if (WITH_C) {
@@ -193,11 +252,11 @@ __device__ __forceinline__ T relax_scale(T target, T sum_f) {
 }
 
 // f at node n as the reference holds it at the start of the step.
-template <typename T, bool RAW>
-__device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const State<T>& s, int n, size_t N,
+template <typename T, typename S, bool RAW, bool USE_POL = false>
+__device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const State<T, S>& s, int n, size_t N,
                                         const Nbr& nb, uint8_t c, T eps, unsigned long long pol = 0ull) {
   const T corr = RAW ? T(1) : s.cbuf[s.c_prev];
-  fetch_pop<T, RAW, !RAW>(v, s.fin, n, N, nb, c, eps, corr, pol);
+  fetch_pop<T, S, RAW, !RAW, true, USE_POL>(v, k, s.fin, s.phi_in, n, N, nb, c, eps, corr, pol);
   if (!RAW && k.relax_on && (c & kTop)) {
     const T r = relax_target(k, ldg(s.phi_in + n), corr);
     if (r >= T(0)) {
@@ -213,8 +272,8 @@ __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const Sta
 // (lbm/fe_ac_solver.py:296-320 fused, :282-294 unfused; fe_wetting.py:418-446).
 // ps[q] holds phi(x + e_q); nsolid(q) tells whether that neighbour is solid.
 // ---------------------------------------------------------------------------
-template <typename T, bool FUSED, typename SolidFn>
-__device__ __forceinline__ void grad_lap(const Consts<T>& k, const State<T>& s, int n, uint8_t c, T phi,
+template <typename T, bool FUSED, typename St, typename SolidFn>
+__device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n, uint8_t c, T phi,
                                          T (&ps)[Q], SolidFn nsolid, T& gx, T& gy, T& gz, T& lap) {
   if (k.wetting && (c & kBoundary)) {
     const size_t N = (size_t)k.N;
@@ -274,9 +333,11 @@ __device__ __forceinline__ T edot(int q, T a0, T a1, T a2) {
 // The collision of one node (lbm/fe_ac_solver.py:392-530), given its phi,
 // gradient and laplacian; writes fout, gout, u, phi_out.
 // ---------------------------------------------------------------------------
-template <typename T, bool RAW, bool FIRST>
-__device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>& s, int n, const Nbr& nb,
-                                             uint8_t c, T phi, T gx, T gy, T gz, T lap, const Pol& pol) {
+template <typename T, typename S, bool RAW, bool FIRST, typename DestPhi>
+__device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T, S>& s, int n, const Nbr& nb,
+                                             uint8_t c, T phi, T gx, T gy, T gz, T lap, const Pol& pol,
+                                             DestPhi dest_phi) {
+  using IO = PopIO<T, S>;
   const size_t N = (size_t)k.N;
   const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
@@ -309,7 +370,7 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>&
   // 3. pressure from the hydrodynamic populations
   const T eps = (c & kPartial) ? s.eps[n] : T(0);
   T g[Q];
-  fetch_pop<T, RAW, false>(g, s.gin, n, N, nb, c, eps, T(1), pol.once);
+  fetch_pop<T, S, RAW, false, false, true>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1), pol.once);
   const T P = seqsum(g);
 
   // 4. non-equilibrium stress with the new P and the old u (:409-413):
@@ -396,7 +457,7 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>&
       const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
       const T geq = P * k.w[q] + k.w[q] * ((ec + ec * ec * T(0.5)) - b);
       const T G = (nsd * k.w[q]) * edot(q, F0, F1, F2);
-      st_pol(s.gout + (q * Nu + nu), (g[q] - om * (g[q] - geq)) + G, pol.once);
+      st_pol(s.gout + (q * Nu + nu), IO::st_g((g[q] - om * (g[q] - geq)) + G, q, k), pol.once);
     }
   }
 
@@ -423,13 +484,14 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>&
   // 8a. phase-field collision (:496-500)
   {
     T f[Q];
-    fetch_f<T, RAW>(f, k, s, n, N, nb, c, eps);
+    fetch_f<T, S, RAW, true>(f, k, s, n, N, nb, c, eps, pol.same);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
       const T feq = phi * (k.w[q] * (((T(1) + ec) + ec * ec * T(0.5)) - b));
       const T src = k.wac3[q] * edot(q, S0, S1, S2);
-      st_pol(s.fout + (q * Nu + nu), (f[q] - k.omega_f * (f[q] - feq)) + src, pol.once);
+      st_pol(s.fout + (q * Nu + nu),
+             IO::st_f((f[q] - k.omega_f * (f[q] - feq)) + src, q, IO::kDev ? dest_phi(q) : T(0), k), pol.once);
     }
   }
   st_pol(s.u + nu, u0, pol.once);
@@ -442,14 +504,16 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T>&
 // The fused time step
 // ---------------------------------------------------------------------------
 // Resident blocks per SM the step kernel is compiled for: three for float
-// (80 registers, no spills), one for double (no spills at double width).
-template <typename T>
+// populations (80 registers), two for half populations (the deviation
+// decoding needs more registers; half the bytes need less parallelism), one
+// for double.
+template <typename T, typename S>
 struct StepOccupancy {
-  static constexpr int blocks = sizeof(T) == 4 ? 3 : 1;
+  static constexpr int blocks = sizeof(T) == 8 ? 1 : (sizeof(S) == 2 ? 2 : 3);
 };
 
-template <typename T, bool RAW, bool FIRST>
-__global__ void __launch_bounds__(kBlock, StepOccupancy<T>::blocks) k_step(Consts<T> k, State<T> s, Tiling tl) {
+template <typename T, typename S, bool RAW, bool FIRST>
+__global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Consts<T> k, State<T, S> s, Tiling tl) {
   // shared memory: phi and node class of the tile and its halo
   extern __shared__ __align__(16) unsigned char smem[];
   T* sphi = reinterpret_cast<T*>(smem);
@@ -492,7 +556,7 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T>::blocks) k_step(Const
       if (!(c & kSolid)) {
         const T eps = (c & kPartial) ? s.eps[n] : T(0);
         T v[Q];
-        fetch_f<T, RAW>(v, k, s, n, N, nbc, c, eps, pol.keep);
+        fetch_f<T, S, RAW, true>(v, k, s, n, N, nbc, c, eps, pol.keep);
         phi = clamp01(seqsum(v));
       }
       sphi[h] = phi;
@@ -517,7 +581,7 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T>::blocks) k_step(Const
         const Nbr nb = make_nbr_xyz(gx, gy, gz, k.nx, k.ny, k.nz);
         const T eps = (c & kPartial) ? s.eps[n] : T(0);
         T v[Q];
-        fetch_f<T, RAW>(v, k, s, n, N, nb, c, eps, pol.keep);
+        fetch_f<T, S, RAW, true>(v, k, s, n, N, nb, c, eps, pol.keep);
         phi = clamp01(seqsum(v));
       }
       sphi[h] = phi;
@@ -564,7 +628,10 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T>::blocks) k_step(Const
                       [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; },
                       gx, gy, gz, lap);
     const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
-    collide_node<T, RAW, FIRST>(k, s, n, nb, c, phi, gx, gy, gz, lap, pol);
+    // phi of this step at x + e_q: the next step's reader of slot (x, q) uses
+    // it as the deviation reference of the half form
+    collide_node<T, S, RAW, FIRST>(k, s, n, nb, c, phi, gx, gy, gz, lap, pol,
+                                   [&](int q) { return sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)]; });
   }
 }
 
@@ -572,8 +639,9 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T>::blocks) k_step(Const
 // init_fields (lbm/fe_ac_solver.py:239-261): phi = clamp(phi0), f = f_eq,
 // g = g_eq(0, u), phi-mass reference.
 // ---------------------------------------------------------------------------
-template <typename T, typename S>
-__global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T> s, const S* phi0, const S* u0) {
+template <typename T, typename S, typename Src>
+__global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T, S> s, const Src* phi0, const Src* u0) {
+  using IO = PopIO<T, S>;
   const int n = blockIdx.x * kBlock + threadIdx.x;
   const size_t N = (size_t)k.N;
   double part = 0.0;
@@ -581,13 +649,14 @@ __global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T> s, const 
     const T phi = clamp01((T)phi0[n]);
     const T v0 = u0 ? (T)u0[n] : T(0), v1 = u0 ? (T)u0[N + n] : T(0), v2 = u0 ? (T)u0[2 * N + n] : T(0);
     const T b = ((v0 * v0 + v1 * v1) + v2 * v2) / k.two_cs2;
-    T* f = const_cast<T*>(s.fin);
-    T* g = const_cast<T*>(s.gin);
+    S* f = const_cast<S*>(s.fin);
+    S* g = const_cast<S*>(s.gin);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const T ec = edot(q, v0, v1, v2) / k.cs2;
-      f[(size_t)q * N + n] = phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b));
-      g[(size_t)q * N + n] = T(0) * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b);
+      // the state right after init is read in place (RAW): deviation reference = own phi
+      f[(size_t)q * N + n] = IO::st_f(phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b)), q, phi, k);
+      g[(size_t)q * N + n] = IO::st_g(T(0) * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b), q, k);
     }
     s.u[n] = v0;
     s.u[N + n] = v1;
@@ -611,8 +680,8 @@ __global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T> s, const 
 // ---------------------------------------------------------------------------
 enum ObserveMode { kObsInit = 0, kObsStep = 1 };
 
-template <typename T, bool RAW_IN>
-__global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T> s, unsigned mask, int mode,
+template <typename T, typename S, bool RAW_IN>
+__global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, unsigned mask, int mode,
                                                     T* phi_o, T* rho_o, T* u_o, T* P_o, T* p_o, T* mu_o) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
   if (n >= k.N) return;
@@ -646,7 +715,7 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T> s, uns
       if (mode == kObsStep) {
         const T eps = (c & kPartial) ? s.eps[n] : T(0);
         T g[Q];
-        fetch_pop<T, RAW_IN, false>(g, s.gin, n, N, nb, c, eps, T(1));
+        fetch_pop<T, S, RAW_IN, false, false>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
         P = seqsum(g);
       }
       if (mask & 8u) P_o[n] = P;
@@ -667,8 +736,8 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T> s, uns
 
 // Current populations in the reference layout: s.fin/s.gin hold the last
 // step's output, s.phi_in that step's phi and s.c_prev its correction.
-template <typename T, bool RAW>
-__global__ void __launch_bounds__(kBlock) k_populations(Consts<T> k, State<T> s, T* f_o, T* g_o) {
+template <typename T, typename S, bool RAW>
+__global__ void __launch_bounds__(kBlock) k_populations(Consts<T> k, State<T, S> s, T* f_o, T* g_o) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
   if (n >= k.N) return;
   const size_t N = (size_t)k.N;
@@ -678,12 +747,12 @@ __global__ void __launch_bounds__(kBlock) k_populations(Consts<T> k, State<T> s,
   const T eps = (c & kPartial) ? s.eps[n] : T(0);
   T v[Q];
   if (f_o) {
-    fetch_f<T, RAW>(v, k, s, n, N, nb, c, eps);
+    fetch_f<T, S, RAW>(v, k, s, n, N, nb, c, eps);
 #pragma unroll
     for (int q = 0; q < Q; ++q) f_o[(size_t)q * N + n] = v[q];
   }
   if (g_o) {
-    fetch_pop<T, RAW, false>(v, s.gin, n, N, nb, c, eps, T(1));
+    fetch_pop<T, S, RAW, false, false>(v, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
 #pragma unroll
     for (int q = 0; q < Q; ++q) g_o[(size_t)q * N + n] = v[q];
   }
@@ -802,50 +871,48 @@ size_t step_smem_bytes(const Tiling& tl) {
   return (size_t)tl.hmax * (sizeof(T) + 1);
 }
 
-template <typename T, bool RAW, bool FIRST>
-static cudaError_t launch_step_t(const Consts<T>& k, const State<T>& s, const Tiling& tl, cudaStream_t st) {
+template <typename T, typename S, bool RAW, bool FIRST>
+static cudaError_t launch_step_t(const Consts<T>& k, const State<T, S>& s, const Tiling& tl, cudaStream_t st) {
   const size_t sm = step_smem_bytes<T>(tl);
-  auto fn = k_step<T, RAW, FIRST>;
+  auto fn = k_step<T, S, RAW, FIRST>;
   if (sm > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
   }
   fn<<<tl.ntx * tl.nty * tl.ntz, kBlock, sm, st>>>(k, s, tl);
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_step(const Consts<T>& k, const State<T>& s, const Tiling& tl, bool raw, bool first,
+template <typename T, typename S>
+cudaError_t launch_step(const Consts<T>& k, const State<T, S>& s, const Tiling& tl, bool raw, bool first,
                         cudaStream_t st) {
-  if (raw && first) return launch_step_t<T, true, true>(k, s, tl, st);
-  if (raw) return launch_step_t<T, true, false>(k, s, tl, st);
-  if (first) return launch_step_t<T, false, true>(k, s, tl, st);
-  return launch_step_t<T, false, false>(k, s, tl, st);
+  if (raw && first) return launch_step_t<T, S, true, true>(k, s, tl, st);
+  if (raw) return launch_step_t<T, S, true, false>(k, s, tl, st);
+  if (first) return launch_step_t<T, S, false, true>(k, s, tl, st);
+  return launch_step_t<T, S, false, false>(k, s, tl, st);
+}
+
+template <typename T, typename S, typename Src>
+cudaError_t launch_init(const Consts<T>& k, const State<T, S>& s, const Src* phi0, const Src* u0, cudaStream_t st) {
+  const int grid = (k.N + kBlock - 1) / kBlock;
+  k_init<T, S, Src><<<grid, kBlock, 0, st>>>(k, s, phi0, u0);
+  return cudaGetLastError();
 }
 
 template <typename T, typename S>
-cudaError_t launch_init(const Consts<T>& k, const State<T>& s, const S* phi0, const S* u0, cudaStream_t st) {
-  const int grid = (k.N + kBlock - 1) / kBlock;
-  k_init<T, S><<<grid, kBlock, 0, st>>>(k, s, phi0, u0);
-  return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t launch_observe(const Consts<T>& k, const State<T>& s, bool raw_in, unsigned mask, int mode,
+cudaError_t launch_observe(const Consts<T>& k, const State<T, S>& s, bool raw_in, unsigned mask, int mode,
                            T* phi, T* rho, T* u, T* P, T* p, T* mu, cudaStream_t st) {
   const int grid = (k.N + kBlock - 1) / kBlock;
-  if (raw_in) k_observe<T, true><<<grid, kBlock, 0, st>>>(k, s, mask, mode, phi, rho, u, P, p, mu);
-  else k_observe<T, false><<<grid, kBlock, 0, st>>>(k, s, mask, mode, phi, rho, u, P, p, mu);
+  if (raw_in) k_observe<T, S, true><<<grid, kBlock, 0, st>>>(k, s, mask, mode, phi, rho, u, P, p, mu);
+  else k_observe<T, S, false><<<grid, kBlock, 0, st>>>(k, s, mask, mode, phi, rho, u, P, p, mu);
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_populations(const Consts<T>& k, const State<T>& s, bool raw, T* f, T* g, cudaStream_t st) {
+template <typename T, typename S>
+cudaError_t launch_populations(const Consts<T>& k, const State<T, S>& s, bool raw, T* f, T* g, cudaStream_t st) {
   const int grid = (k.N + kBlock - 1) / kBlock;
-  if (raw) k_populations<T, true><<<grid, kBlock, 0, st>>>(k, s, f, g);
-  else k_populations<T, false><<<grid, kBlock, 0, st>>>(k, s, f, g);
+  if (raw) k_populations<T, S, true><<<grid, kBlock, 0, st>>>(k, s, f, g);
+  else k_populations<T, S, false><<<grid, kBlock, 0, st>>>(k, s, f, g);
   return cudaGetLastError();
 }
 
@@ -861,16 +928,23 @@ cudaError_t launch_measure(int nx, int ny, int nz, const T* phi, const uint8_t* 
 
 template size_t step_smem_bytes<float>(const Tiling&);
 template size_t step_smem_bytes<double>(const Tiling&);
-template cudaError_t launch_step<float>(const Consts<float>&, const State<float>&, const Tiling&, bool, bool, cudaStream_t);
-template cudaError_t launch_step<double>(const Consts<double>&, const State<double>&, const Tiling&, bool, bool, cudaStream_t);
-template cudaError_t launch_init<float, float>(const Consts<float>&, const State<float>&, const float*, const float*, cudaStream_t);
-template cudaError_t launch_init<float, double>(const Consts<float>&, const State<float>&, const double*, const double*, cudaStream_t);
-template cudaError_t launch_init<double, float>(const Consts<double>&, const State<double>&, const float*, const float*, cudaStream_t);
-template cudaError_t launch_init<double, double>(const Consts<double>&, const State<double>&, const double*, const double*, cudaStream_t);
-template cudaError_t launch_observe<float>(const Consts<float>&, const State<float>&, bool, unsigned, int, float*, float*, float*, float*, float*, float*, cudaStream_t);
-template cudaError_t launch_observe<double>(const Consts<double>&, const State<double>&, bool, unsigned, int, double*, double*, double*, double*, double*, double*, cudaStream_t);
-template cudaError_t launch_populations<float>(const Consts<float>&, const State<float>&, bool, float*, float*, cudaStream_t);
-template cudaError_t launch_populations<double>(const Consts<double>&, const State<double>&, bool, double*, double*, cudaStream_t);
+
+#define LBM_INSTANTIATE(T, S)                                                                                   \
+  template cudaError_t launch_step<T, S>(const Consts<T>&, const State<T, S>&, const Tiling&, bool, bool,        \
+                                         cudaStream_t);                                                          \
+  template cudaError_t launch_init<T, S, float>(const Consts<T>&, const State<T, S>&, const float*, const float*,  \
+                                                cudaStream_t);                                                   \
+  template cudaError_t launch_init<T, S, double>(const Consts<T>&, const State<T, S>&, const double*,             \
+                                                 const double*, cudaStream_t);                                    \
+  template cudaError_t launch_observe<T, S>(const Consts<T>&, const State<T, S>&, bool, unsigned, int, T*, T*, T*, \
+                                            T*, T*, T*, cudaStream_t);                                           \
+  template cudaError_t launch_populations<T, S>(const Consts<T>&, const State<T, S>&, bool, T*, T*, cudaStream_t);
+
+LBM_INSTANTIATE(float, float)
+LBM_INSTANTIATE(double, double)
+LBM_INSTANTIATE(float, __half)
+#undef LBM_INSTANTIATE
+
 template cudaError_t launch_measure<float>(int, int, int, const float*, const uint8_t*, double*, int, unsigned*, double*, cudaStream_t);
 template cudaError_t launch_measure<double>(int, int, int, const double*, const uint8_t*, double*, int, unsigned*, double*, cudaStream_t);
 

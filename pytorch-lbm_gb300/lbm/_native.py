@@ -13,7 +13,7 @@ import torch  # noqa: F401  (loads the CUDA runtime the library links against)
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "liblbm_gb300.so")
 
-LBM_F32, LBM_F64 = 0, 1
+LBM_F32, LBM_F64, LBM_F16 = 0, 1, 2
 LBM_DT_NONE, LBM_DT_F32, LBM_DT_F64 = 0, 1, 2
 FIELD_PHI, FIELD_RHO, FIELD_U, FIELD_P, FIELD_PRESS, FIELD_MU = 1, 2, 4, 8, 16, 32
 STATUS_NAN, STATUS_MASS_LOW = 1, 2

@@ -87,8 +87,8 @@ class AllenCahnSolver:
             raise NotImplementedError("direct_wetting is not supported")
         if torch.is_tensor(geo_amplification) or isinstance(geo_amplification, np.ndarray):
             raise NotImplementedError("per-node geo_amplification is not supported")
-        if dtype not in (torch.float32, torch.float64):
-            raise ValueError("dtype must be torch.float32 or torch.float64")
+        if dtype not in (torch.float32, torch.float64, torch.float16):
+            raise ValueError("dtype must be torch.float32, torch.float64 or torch.float16")
         self.config = config
         dev = torch.device(config.device) if not isinstance(config.device, torch.device) else config.device
         if dev.type != "cuda":
@@ -98,7 +98,10 @@ class AllenCahnSolver:
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
         self.device = dev
-        self.dtype = dtype
+        # float16 selects the deviation-storage form: populations in half
+        # precision, arithmetic and the exposed fields in float32
+        self.population_dtype = dtype
+        self.dtype = torch.float32 if dtype == torch.float16 else dtype
         self.step_count = 0
         self.t = 0.0
         self.stab_mode = "fakhari" if stab_mode == "auto" else stab_mode
@@ -133,7 +136,8 @@ class AllenCahnSolver:
             disc = 1.0 - 4.0 * (-c / 3.0)
             self._phi_wall_target = (0.5 * (1.0 - math.sqrt(disc)) if disc >= 0 else
                                      0.5 * (1.0 - math.cos(math.pi - math.radians(config.theta_eq))))
-        self._prec = nat.LBM_F32 if dtype == torch.float32 else nat.LBM_F64
+        self._prec = {torch.float32: nat.LBM_F32, torch.float64: nat.LBM_F64,
+                      torch.float16: nat.LBM_F16}[dtype]
         p = nat.LbmParams()
         for k in ("rho_l", "rho_g", "sigma", "xi", "beta", "kappa", "phi_c", "tau_l", "tau_g",
                   "tau_h", "theta_eq"):
