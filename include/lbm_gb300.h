@@ -182,6 +182,34 @@ int lbm_get_scalars(LbmHandle* h, double* phi_mass_init, double* last_sum_phi,
  * scripts/run_thesis_sweep.py:182-216. */
 int lbm_measure(LbmHandle* h, double* out9, void* stream);
 
+/* Maximum node count of lbm_measure_static (its indexing is 32-bit). */
+#define LBM_MEASURE_STATIC_MAX_NODES (1LL << 30)
+
+/* Spread diagnostics of a caller's phi field that allocate nothing: no
+ * cudaMalloc, no cudaFree, no allocating library call.  For callers that
+ * cannot allocate device memory: code that runs inside a memory pool owned by
+ * another runtime, host code under a driver that forbids allocation after
+ * start-up, or a monitoring hook that must not disturb the allocator of the
+ * solve it observes.  The reduction's block partials and its completion
+ * counter live in a static device array of the library (1024 blocks x 11
+ * doubles, about 90 KB, plus one counter), which every GPU that loads the
+ * library holds until the process exits.
+ *
+ * phi: device, nx*ny*nz elements of phi_dtype (LBM_DT_F32 or LBM_DT_F64);
+ * solid: device, nx*ny*nz bytes, 1 = solid, 0 = fluid (a torch.bool tensor);
+ * out9: device, 9 doubles, written as by lbm_measure (volume, C_max, Dx, Dy,
+ * Dz, k, z centre, count, NaN flag).  Asynchronous on `stream`.  Grids of more
+ * than LBM_MEASURE_STATIC_MAX_NODES nodes are rejected with LBM_E_ARG.
+ *
+ * The first call on a device looks up the static array's device address
+ * (this may load the library's kernels onto that device), so make it before
+ * any stream capture.  Every call shares the one array and leaves its
+ * contents behind: calls that overlap on the GPU (two streams, or two host
+ * threads on one device) race and must be serialised by the caller.  No
+ * counterpart in the reference: an addition of this library. */
+int lbm_measure_static(int64_t nx, int64_t ny, int64_t nz, const void* phi, int phi_dtype,
+                       const uint8_t* solid, double* out9, void* stream);
+
 /* Sticky status flags (LBM_STATUS_*) accumulated by the device; synchronises. */
 int lbm_status(LbmHandle* h, uint32_t* flags);
 

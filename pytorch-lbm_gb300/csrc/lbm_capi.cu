@@ -31,6 +31,8 @@ cudaError_t launch_populations(const Consts<T>&, const State<T, S>&, bool, T*, T
 template <typename T>
 cudaError_t launch_measure(int, int, int, const T*, const uint8_t*, double*, int, unsigned*, double*,
                            cudaStream_t);
+template <typename T>
+cudaError_t launch_measure_static(int, int, int, const T*, const uint8_t*, double*, cudaStream_t);
 }  // namespace lbm
 
 using namespace lbm;
@@ -684,3 +686,25 @@ int lbm_status(LbmHandle* h, uint32_t* flags) {
 }
 
 }  // extern "C"
+
+int lbm_measure_static(int64_t nx, int64_t ny, int64_t nz, const void* phi, int phi_dtype,
+                       const uint8_t* solid, double* out9, void* stream) {
+  if (!phi || !solid || !out9) return fail(LBM_E_ARG, "lbm_measure_static: null argument");
+  if (nx < 1 || ny < 1 || nz < 1) return fail(LBM_E_ARG, "lbm_measure_static: grid extents must be >= 1");
+  if (nx > LBM_MEASURE_STATIC_MAX_NODES || ny > LBM_MEASURE_STATIC_MAX_NODES ||
+      nz > LBM_MEASURE_STATIC_MAX_NODES || nx * ny > LBM_MEASURE_STATIC_MAX_NODES ||
+      nx * ny * nz > LBM_MEASURE_STATIC_MAX_NODES)
+    return fail(LBM_E_ARG, "lbm_measure_static: " + std::to_string(nx) + "x" + std::to_string(ny) + "x" +
+                               std::to_string(nz) + " exceeds the maximum of " +
+                               std::to_string((long long)LBM_MEASURE_STATIC_MAX_NODES) + " nodes");
+  if (phi_dtype != LBM_DT_F32 && phi_dtype != LBM_DT_F64)
+    return fail(LBM_E_ARG, "lbm_measure_static: phi_dtype must be LBM_DT_F32 or LBM_DT_F64");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (phi_dtype == LBM_DT_F32)
+    e = launch_measure_static<float>((int)nx, (int)ny, (int)nz, (const float*)phi, solid, out9, st);
+  else
+    e = launch_measure_static<double>((int)nx, (int)ny, (int)nz, (const double*)phi, solid, out9, st);
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_measure_static: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}

@@ -27,6 +27,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "lbm_common.cuh"
 
 namespace lbm {
@@ -925,6 +927,72 @@ cudaError_t launch_measure(int nx, int ny, int nz, const T* phi, const uint8_t* 
   k_measure<T><<<grid, kBlock, 0, st>>>(nx, ny, nz, phi, cls, partials, counter, out);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free spread diagnostics.  Some callers cannot allocate device
+// memory: code that runs inside a memory pool handed out by another runtime,
+// host code under a driver that forbids cudaMalloc after start-up, or a
+// measurement hook that must not perturb the allocator it observes.  For them
+// the block partials and the completion counter of k_measure live in this
+// file-scope scratch, which every GPU that loads the library holds until the
+// process exits.  Calls share it and it keeps the last call's contents, so
+// calls that overlap on the GPU (different streams, or different host
+// threads on one device) race and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+constexpr int kStaticMeasBlocks = 1024;  // 1024 x 11 doubles = 90,112 bytes of partials
+static __device__ __align__(256) double g_static_meas_partials[kStaticMeasBlocks * kMeasVals];
+static __device__ __align__(256) unsigned g_static_meas_counter;
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+double* g_static_partials_dev[kMaxDevices] = {};
+unsigned* g_static_counter_dev[kMaxDevices] = {};
+}  // namespace
+
+// Device addresses of the static scratch on the current device.  In host
+// code the two arrays' names only denote host-side shadows; the device
+// addresses come from cudaGetSymbolAddress, looked up once per device with
+// that device current (which may load this module onto the device, so the
+// first call on a device should come before any stream capture).
+static cudaError_t static_meas_scratch(double** partials, unsigned** counter) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_partials_dev[dev]) {
+    void* p = nullptr;
+    void* c = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_meas_partials);
+    if (e != cudaSuccess) return e;
+    e = cudaGetSymbolAddress(&c, g_static_meas_counter);
+    if (e != cudaSuccess) return e;
+    g_static_counter_dev[dev] = static_cast<unsigned*>(c);
+    g_static_partials_dev[dev] = static_cast<double*>(p);
+  }
+  *partials = g_static_partials_dev[dev];
+  *counter = g_static_counter_dev[dev];
+  return cudaSuccess;
+}
+
+// k_measure over a caller's phi and 0/1 solid mask with the static scratch;
+// writes the 9 outputs to `out` (device).  No allocation.
+template <typename T>
+cudaError_t launch_measure_static(int nx, int ny, int nz, const T* phi, const uint8_t* solid, double* out,
+                                  cudaStream_t st) {
+  double* partials = nullptr;
+  unsigned* counter = nullptr;
+  cudaError_t e = static_meas_scratch(&partials, &counter);
+  if (e != cudaSuccess) return e;
+  // the counter must start at zero: a launch that failed part-way leaves it set
+  e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  return launch_measure<T>(nx, ny, nz, phi, solid, partials, kStaticMeasBlocks, counter, out, st);
+}
+template cudaError_t launch_measure_static<float>(int, int, int, const float*, const uint8_t*, double*, cudaStream_t);
+template cudaError_t launch_measure_static<double>(int, int, int, const double*, const uint8_t*, double*,
+                                                   cudaStream_t);
 
 template size_t step_smem_bytes<float>(const Tiling&);
 template size_t step_smem_bytes<double>(const Tiling&);
