@@ -121,15 +121,20 @@ int lbm_step(LbmHandle* h, int nsteps, void* stream);
  * measurement; same results as lbm_step. */
 int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3);
 
-/* Tile extents (x, y, z) of the fused step kernel; 0 = automatic, else 2..64
- * for x and y and 2..256 for z.  Results do not depend on the tiling; speed
- * does.  No reference counterpart (a GB300 launch parameter). */
+/* Step kernel selection.  (0, 0, 0), the default, selects the two-kernel
+ * streaming step (k_phi: phi and its grid sum, one thread per node; k_update:
+ * the rest of the step, reading the phi stencil from L2).  Other extents
+ * select the fused tiled kernel (one launch per step, phi recomputed on a
+ * one-node halo in shared memory) with those tile extents, 2..64 for x and y
+ * and 2..256 for z (an extent given as 0 is chosen automatically).  Results do
+ * not depend on the choice; speed does.  lbm_get_tile returns (0, 0, 0) for
+ * the two-kernel step.  No reference counterpart (a GB300 launch parameter). */
 int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz);
 int lbm_get_tile(LbmHandle* h, int* txyz3);
 
-/* Tile autotuner: times `reps` launches of the next step kernel for each
- * candidate tile shape on the handle's current state (which it leaves
- * unchanged) and keeps the fastest.  Synchronises `stream`; allocates a
+/* Step autotuner: times `reps` launches of the next step for the two-kernel
+ * step and for each candidate tile shape of the fused kernel on the handle's
+ * current state (which it leaves unchanged) and keeps the fastest.  Synchronises `stream`; allocates a
  * temporary copy of u.  Outputs (may be NULL): the chosen extents and its
  * time per launch in ms.  No reference counterpart. */
 int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* best_ms);

@@ -17,7 +17,7 @@
 #include "lbm_tables.h"
 
 namespace lbm {
-template <typename T>
+template <typename T, typename S>
 size_t step_smem_bytes(const Tiling&);
 template <typename T, typename S>
 cudaError_t launch_step(const Consts<T>&, const State<T, S>&, const Tiling&, bool, bool, cudaStream_t);
@@ -58,6 +58,7 @@ struct LbmHandle {
   LbmParams prm;
   int prec = LBM_F32;
   int64_t nx = 0, ny = 0, nz = 0, N = 0;
+  int64_t Np = 0;  // component stride of f, g, u: N rounded up to kAlignNodes
   int device = 0;
   size_t tsize = 4;  // compute type (u, phi, eps, fields)
   size_t psize = 4;  // population storage type
@@ -102,6 +103,9 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   k.ny = (int)h.ny;
   k.nz = (int)h.nz;
   k.N = (int)h.N;
+  k.Np = (int)h.Np;
+  k.dz = make_fastdiv((unsigned)h.nz);
+  k.dy = make_fastdiv((unsigned)h.ny);
   const double cs2 = 1.0 / 3.0;
   const double tau_f = p.tau_h > 0 ? p.tau_h : p.tau_l;
   const double ac_coeff = 1.0 - 0.5 / tau_f;
@@ -238,14 +242,22 @@ Tiling tiling_of(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz) {
 }
 
 size_t tiling_smem(const Tiling& t, int prec) {
-  return prec == LBM_F64 ? step_smem_bytes<double>(t) : step_smem_bytes<float>(t);
+  if (t.tx == 0) return 0;
+  if (prec == LBM_F64) return step_smem_bytes<double, double>(t);
+  if (prec == LBM_F16) return step_smem_bytes<float, __half>(t);
+  return step_smem_bytes<float, float>(t);
 }
 
-// Default tiling of the fused step: z extent balanced over nz near 28 and a
-// 6 x 6 x-y cross-section (the shape the autotuner picks on the 150x150x107
-// ridge case).  Explicit extents (> 0) are taken as given.
+// Step kernels: all extents 0 selects the two-kernel streaming step (the
+// default); otherwise the fused tiled kernel, with a z extent balanced over nz
+// near 28 and a 6 x 6 x-y cross-section for the extents given as 0.
 Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz, int prec) {
   (void)prec;
+  if (tx <= 0 && ty <= 0 && tz <= 0) {
+    Tiling t;
+    std::memset(&t, 0, sizeof(t));
+    return t;
+  }
   if (tz <= 0) {
     const int ntz = (int)((nz + 27) / 28);
     tz = (int)((nz + ntz - 1) / ntz);
@@ -324,7 +336,8 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   if (precision != LBM_F32 && precision != LBM_F64 && precision != LBM_F16)
     return fail(LBM_E_ARG, "lbm_create: precision must be LBM_F32, LBM_F64 or LBM_F16");
   const int64_t N = nx * ny * nz;
-  if (N * Q > (int64_t)0x7fffffff) return fail(LBM_E_ARG, "lbm_create: grid too large (19 N must be < 2^31)");
+  const int64_t Np = (N + kAlignNodes - 1) / kAlignNodes * kAlignNodes;
+  if (Np * Q > (int64_t)0x7fffffff) return fail(LBM_E_ARG, "lbm_create: grid too large (19 N must be < 2^31)");
   if (params->stab_mode < 0 || params->stab_mode > 2) return fail(LBM_E_ARG, "lbm_create: bad stab_mode");
   if (!(params->tau_g > 0.5) || !(params->tau_l > 0.5)) return fail(LBM_E_ARG, "lbm_create: tau_l, tau_g must exceed 0.5");
   if (!(params->xi > 0)) return fail(LBM_E_ARG, "lbm_create: xi must be positive");
@@ -336,6 +349,7 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   h->ny = ny;
   h->nz = nz;
   h->N = N;
+  h->Np = Np;
   h->tsize = precision == LBM_F64 ? 8 : 4;
   h->psize = precision == LBM_F64 ? 8 : (precision == LBM_F16 ? 2 : 4);
   h->wetting = params->theta_eq != 90.0 && params->kappa > 0;
@@ -352,10 +366,10 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
     if (e == cudaSuccess) e = cudaMalloc(p, bytes);
   };
   for (int b = 0; b < 2; ++b) {
-    A(&h->f[b], (size_t)Q * N * h->psize);
-    A(&h->g[b], (size_t)Q * N * h->psize);
+    A(&h->f[b], (size_t)Q * Np * h->psize);
+    A(&h->g[b], (size_t)Q * Np * h->psize);
   }
-  A(&h->u, 3 * N * T);
+  A(&h->u, 3 * Np * T);
   A(&h->phi[0], N * T);
   A(&h->phi[1], N * T);
   A(&h->eps, N * T);
@@ -498,7 +512,7 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_autotune: call lbm_init_fields first");
   if (reps <= 0) reps = 5;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const size_t ub = 3 * (size_t)h->N * h->tsize;
+  const size_t ub = 3 * (size_t)h->Np * h->tsize;
   void* u_save = nullptr;
   CUDA_TRY(cudaMalloc(&u_save, ub));
   CUDA_TRY(cudaMemcpyAsync(u_save, h->u, ub, cudaMemcpyDeviceToDevice, st));
@@ -508,6 +522,7 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
   // candidate tiles: z extents balanced over nz near 32 / 48 / 64, square
   // x-y cross-sections of 4..16 nodes, shared memory within a third of an SM
   std::vector<Tiling> cands;
+  cands.push_back(make_tiling(h->nx, h->ny, h->nz, 0, 0, 0, h->prec));  // two-kernel step
   for (int zt : {24, 32, 48, 64}) {
     const int ntz = (int)((h->nz + zt - 1) / zt);
     const int tz = (int)((h->nz + ntz - 1) / ntz);

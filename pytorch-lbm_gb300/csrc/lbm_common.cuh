@@ -88,12 +88,37 @@ __device__ __forceinline__ Nbr make_nbr(int n, int nx, int ny, int nz, int* ix_o
   return b;
 }
 
+// Exact n / d for 0 <= n < 2^31 and 1 <= d < 2^31 by a multiply-high and a
+// shift (division by an invariant integer, Granlund & Montgomery 1994):
+// with l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> l.
+struct FastDiv {
+  unsigned d, m, l;
+  __device__ __forceinline__ unsigned div(unsigned n) const { return (__umulhi(n, m) + n) >> l; }
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  f.d = d;
+  f.l = 0;
+  while ((1ull << f.l) < d) ++f.l;
+  f.m = (unsigned)((((1ull << f.l) - d) << 32) / d + 1ull);
+  return f;
+}
+
+// Population arrays (f, g) and u store component j of node n at j * Np + n,
+// Np = N rounded up to a multiple of kAlignNodes, so that every component
+// array starts on a 128-byte line and a warp's 32 consecutive nodes of one
+// component fill whole lines.  Caller-facing arrays are dense (j * N + n).
+constexpr int kAlignNodes = 32;
+
 // Constants of one grid's time step in the compute type T.  Every value is
 // the reference's python-double expression rounded once to T at the point the
 // reference mixes it into a T tensor.
 template <typename T>
 struct Consts {
   int nx, ny, nz, N;
+  int Np;             // component stride of f, g and u (N rounded up to kAlignNodes)
+  FastDiv dz, dy;     // division by nz and by ny
   T w[Q];      // lattice weights (float32 table, widened)
   T wc[Q];     // w_i / cs2                      (stencil weights)
   T w2c[Q];    // 2 w_i / cs2                    (laplacian weights)
@@ -131,7 +156,7 @@ struct State {
   S* gout;
   T* u;           // velocity [3][N], in place
   const T* phi_in;  // phi recovered by the last step (before its mass correction)
-  T* phi_out;       // phi recovered by this step
+  T* phi_out;       // phi recovered by this step (written by the phi kernel in the two-kernel step)
   const uint8_t* cls;
   const float* wn;  // wall normal [3][N] (non-zero at boundary nodes only)
   const T* eps;     // solid fraction (read at partial nodes only)

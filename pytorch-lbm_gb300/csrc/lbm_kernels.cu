@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "lbm_common.cuh"
 
@@ -81,6 +82,22 @@ __device__ __forceinline__ __half ld_pol(const __half* p, unsigned long long pol
 }
 __device__ __forceinline__ void st_pol(__half* p, __half v, unsigned long long pol) {
   asm volatile("st.global.L2::cache_hint.b16 [%0], %1, %2;" ::"l"(p), "h"(__half_as_ushort(v)), "l"(pol));
+}
+
+// Asynchronous global -> shared copies of one 4- or 8-byte element (no
+// register holds the value in flight), with an L2 policy.
+template <typename T>
+__device__ __forceinline__ void cp_async(T* sdst, const T* gsrc, unsigned long long pol) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cp.async copies 4, 8 or 16 bytes");
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], %2, %3;" ::"r"(sa), "l"(gsrc),
+               "n"(sizeof(T)), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
 }
 
 // Population storage.  S == T stores the population itself.  S == half (the
@@ -194,8 +211,9 @@ __device__ __forceinline__ void fetch_pop(T (&v)[Q], const Consts<T>& k, const S
                                           const T* __restrict__ phi_in, int n, size_t N, const Nbr& nb,
                                           uint8_t c, T eps, T corr, unsigned long long pol = 0ull) {
   using IO = PopIO<T, S>;
-  // element offsets q N + m stay below 2^31 (checked when the grid is created)
-  const unsigned Nu = (unsigned)N, nu = (unsigned)n;
+  // element offsets q Np + m stay below 2^31 (checked when the grid is created)
+  const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+  (void)N;
   const T ref_self = (IO::kDev && IS_F) ? ldg(phi_in + n) : T(0);
   auto ld = [&](int q, unsigned idx, T ref) -> T {
     const S raw = ld_sel<USE_POL>(F + idx, pol);
@@ -332,15 +350,97 @@ __device__ __forceinline__ T edot(int q, T a0, T a1, T a2) {
 }
 
 // ---------------------------------------------------------------------------
-// The collision of one node (lbm/fe_ac_solver.py:392-530), given its phi,
-// gradient and laplacian; writes fout, gout, u, phi_out.
+// The update of one node (lbm/fe_ac_solver.py:392-530): stencils, chemical
+// potential, wetting, pressure, stress, forces, velocity, Allen-Cahn source
+// and both BGK collisions; writes fout, gout, u, phi_out.
 // ---------------------------------------------------------------------------
-template <typename T, typename S, bool RAW, bool FIRST, typename DestPhi>
-__device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T, S>& s, int n, const Nbr& nb,
-                                             uint8_t c, T phi, T gx, T gy, T gz, T lap, const Pol& pol,
-                                             DestPhi dest_phi) {
+// First population of each opposite pair (q, opp q) of D3Q19.
+__host__ __device__ constexpr int pair_first(int i) {
+  return i == 0 ? 1 : i == 1 ? 3 : i == 2 ? 5 : i == 3 ? 7 : i == 4 ? 8 : i == 5 ? 11 : i == 6 ? 12 : i == 7 ? 15 : 16;
+}
+
+template <typename T>
+__device__ __forceinline__ T fma_(T a, T b, T c) { return fma(a, b, c); }
+
+// OMEGA1: tau_f == 1 (the reference's default tau_h = 1.0), where the
+// phase-field BGK collision f - (f - f_eq) + src is f_eq + src and the
+// pre-collision f is not read.  PhiAt(q) gives phi(x + e_q) of this step,
+// SolidAt(q) whether x + e_q is solid.
+// Words of one node's staging slot: the 19 streamed g, u of the last step, phi
+// of the last step.
+constexpr int kStage = Q + 4;
+
+// Start the asynchronous copies of the g pulled from the neighbours (the
+// streamed values of a fluid node; solid and partial nodes patch them with
+// their own values when used, so no node class is needed here), u and the
+// previous phi of node n into a staging slot (word j at st[j * kBlock]).
+template <typename T, bool RAW, bool FIRST>
+__device__ __forceinline__ void stage_node(const Consts<T>& k, const State<T, T>& s, int n, const Nbr& nb,
+                                           T* st, unsigned long long pol) {
+  const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+  if (RAW) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) cp_async(st + q * kBlock, s.gin + (q * Nu + nu), pol);
+  } else {
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+      cp_async(st + q * kBlock, s.gin + (q * Nu + (unsigned)nb.at(n, -ex(q), -ey(q), -ez(q))), pol);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) cp_async(st + (Q + d) * kBlock, s.u + (d * Nu + nu), pol);
+  if (!FIRST) cp_async(st + (Q + 3) * kBlock, s.phi_in + nu, pol);
+}
+
+// STAGED: g, u and the previous phi come from the node's staging slot `st`
+// (float and double populations); otherwise they are loaded here.
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool STAGED, bool STORE_PHI, typename PhiAt,
+          typename SolidAt>
+__device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S>& s, int n, const Nbr& nb,
+                                            uint8_t c, T phi, PhiAt phi_at, SolidAt solid_at, const Pol& pol,
+                                            const T* st) {
   using IO = PopIO<T, S>;
   const size_t N = (size_t)k.N;
+  const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+
+  // loads that do not depend on the stencil first, so that their latency
+  // overlaps it: g (pulled), u and phi of the last step
+  const T eps = (c & kPartial) ? s.eps[n] : T(0);
+  T g[Q];
+  T uo0, uo1, uo2, pp;
+  if constexpr (STAGED) {
+    const T* gin = reinterpret_cast<const T*>(s.gin);
+    if (!RAW && (c & kSolid)) {
+      // bounce-back: the node's own opposite values, not the staged pulled ones
+#pragma unroll
+      for (int q = 0; q < Q; ++q) g[q] = ldg(gin + (opp(q) * Nu + nu));
+    } else {
+#pragma unroll
+      for (int q = 0; q < Q; ++q) g[q] = st[q * kBlock];
+    }
+    if (!RAW && (c & kPartial)) {
+      const T one_m = T(1) - eps;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) g[q] = one_m * g[q] + eps * ldg(gin + (opp(q) * Nu + nu));
+    }
+    uo0 = st[Q * kBlock];
+    uo1 = st[(Q + 1) * kBlock];
+    uo2 = st[(Q + 2) * kBlock];
+    pp = FIRST ? T(0) : st[(Q + 3) * kBlock];
+  } else {
+    fetch_pop<T, S, RAW, false, false, true>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1), pol.once);
+    uo0 = ld_pol(s.u + nu, pol.once);
+    uo1 = ld_pol(s.u + (Nu + nu), pol.once);
+    uo2 = ld_pol(s.u + (2 * Nu + nu), pol.once);
+    pp = FIRST ? T(0) : ld_pol(s.phi_in + n, pol.once);
+  }
+
+  // 2. gradient and laplacian with the ghost-node wetting values
+  T ps[Q];
+#pragma unroll
+  for (int q = 1; q < Q; ++q) ps[q] = phi_at(q);
+  T gx, gy, gz, lap;
+  grad_lap<T, true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
+
   const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
   const T mu = chem_pot(k, c, phi, lap);
@@ -370,18 +470,12 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T, 
   }
 
   // 3. pressure from the hydrodynamic populations
-  const T eps = (c & kPartial) ? s.eps[n] : T(0);
-  T g[Q];
-  fetch_pop<T, S, RAW, false, false, true>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1), pol.once);
   const T P = seqsum(g);
 
   // 4. non-equilibrium stress with the new P and the old u (:409-413):
   // sum_q e_a e_b (g_q - g_eq_q) = Pi_ab - P cs2 delta_ab - u_a u_b, since the
   // D3Q19 weights satisfy sum w e_a e_b = cs2 delta_ab and
   // sum w e_a e_b e_c e_d = cs2^2 (delta_ab delta_cd + delta_ac delta_bd + delta_ad delta_bc).
-  const unsigned Nu = (unsigned)N, nu = (unsigned)n;
-  const T uo0 = ld_pol(s.u + nu, pol.once), uo1 = ld_pol(s.u + (Nu + nu), pol.once),
-          uo2 = ld_pol(s.u + (2 * Nu + nu), pol.once);
   T sxx, syy, szz, sxy, sxz, syz;
   {
     bool fxx = true, fyy = true, fzz = true, fxy = true, fxz = true, fyz = true;
@@ -442,33 +536,11 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T, 
   }
   const T b = ((u0 * u0 + u1 * u1) + u2 * u2) * k.inv_two_cs2;
 
-  // 8b. hydrodynamic collision (:503-530), before the phase-field one so that
-  // the 19 g values are dead before the 19 f values are loaded
-  {
-    T om;
-    if (k.tau_const) {
-      om = k.omega_g;
-    } else {
-      const T eta = phi * k.rho_l * k.tl_m + (T(1) - phi) * k.rho_g * k.tg_m;
-      const T rden = phi * k.rho_l + (T(1) - phi) * k.rho_g;
-      om = rcp(T(0.5) + eta / rden);
-    }
-    const T nsd = (T(1) - om * T(0.5)) * rcp(rho_eff * k.cs2);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
-      const T geq = P * k.w[q] + k.w[q] * ((ec + ec * ec * T(0.5)) - b);
-      const T G = (nsd * k.w[q]) * edot(q, F0, F1, F2);
-      st_pol(s.gout + (q * Nu + nu), IO::st_g((g[q] - om * (g[q] - geq)) + G, q, k), pol.once);
-    }
-  }
-
   // 7. Allen-Cahn source (:450-494)
   T S0, S1, S2;
   {
     T d0 = T(0), d1 = T(0), d2 = T(0);
     if (!FIRST) {
-      const T pp = ld_pol(s.phi_in + n, pol.once);
       d0 = phi * u0 - pp * uo0;
       d1 = phi * u1 - pp * uo1;
       d2 = phi * u2 - pp * uo2;
@@ -483,23 +555,144 @@ __device__ __forceinline__ void collide_node(const Consts<T>& k, const State<T, 
     S2 = d2 + cl * gz;
   }
 
-  // 8a. phase-field collision (:496-500)
+  // 8. both BGK collisions (:496-530) one opposite pair (q, opp q) at a time.
+  // With ec = e_q.u / cs2 (odd in q) the equilibria split into a part even in
+  // q and a part odd in q:
+  //   g_eq_q = w (P - b + ec^2/2) + w ec,   f_eq_q = phi w (1 - b + ec^2/2) + phi w ec,
+  // and the forcing and Allen-Cahn source terms are odd, so each pair costs
+  // one even and one odd term per lattice.
+  T om;
+  if (k.tau_const) {
+    om = k.omega_g;
+  } else {
+    const T eta = phi * k.rho_l * k.tl_m + (T(1) - phi) * k.rho_g * k.tg_m;
+    const T rden = phi * k.rho_l + (T(1) - phi) * k.rho_g;
+    om = rcp(T(0.5) + eta / rden);
+  }
+  const T omo = T(1) - om;
+  const T nsd = (T(1) - om * T(0.5)) * rcp(rho_eff * k.cs2);
+  const T Pb = P - b;
+  const T omb = T(1) - b;
+  const T pf = OMEGA1 ? phi : k.omega_f * phi;  // omega_f phi
+  const T u3x = u0 * k.inv_cs2, u3y = u1 * k.inv_cs2, u3z = u2 * k.inv_cs2;
+  T f[Q];
+  if (!OMEGA1) fetch_f<T, S, RAW, true>(f, k, s, n, N, nb, c, eps, pol.same);
+  auto store_g = [&](int q, T v) { st_pol(s.gout + (q * Nu + nu), IO::st_g(v, q, k), pol.once); };
+  auto store_f = [&](int q, T v) {
+    st_pol(s.fout + (q * Nu + nu), IO::st_f(v, q, IO::kDev ? phi_at(q) : T(0), k), pol.once);
+  };
   {
-    T f[Q];
-    fetch_f<T, S, RAW, true>(f, k, s, n, N, nb, c, eps, pol.same);
+    const T ow = om * k.w[0];
+    store_g(0, fma_(omo, g[0], ow * Pb));
+    const T pw = pf * k.w[0];
+    const T f0 = pw * omb;
+    store_f(0, OMEGA1 ? f0 : fma_(T(1) - k.omega_f, f[0], f0));
+  }
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const T ec = edot(q, u0, u1, u2) * k.inv_cs2;
-      const T feq = phi * (k.w[q] * (((T(1) + ec) + ec * ec * T(0.5)) - b));
-      const T src = k.wac3[q] * edot(q, S0, S1, S2);
-      st_pol(s.fout + (q * Nu + nu),
-             IO::st_f((f[q] - k.omega_f * (f[q] - feq)) + src, q, IO::kDev ? dest_phi(q) : T(0), k), pol.once);
+  for (int i = 0; i < 9; ++i) {
+    const int q = pair_first(i), p = opp(q);
+    const T wq = k.w[q];
+    const T ec = edot(q, u3x, u3y, u3z);
+    // hydrodynamic pair
+    const T ow = om * wq;
+    const T ge = fma_((T(0.5) * ow) * ec, ec, ow * Pb);
+    const T go = fma_(ow, ec, (nsd * wq) * edot(q, F0, F1, F2));
+    store_g(q, fma_(omo, g[q], ge + go));
+    store_g(p, fma_(omo, g[p], ge - go));
+    // phase-field pair
+    const T pw = pf * wq;
+    const T fe = fma_((T(0.5) * pw) * ec, ec, pw * omb);
+    const T fo = fma_(pw, ec, k.wac3[q] * edot(q, S0, S1, S2));
+    if (OMEGA1) {
+      store_f(q, fe + fo);
+      store_f(p, fe - fo);
+    } else {
+      const T omf = T(1) - k.omega_f;
+      store_f(q, fma_(omf, f[q], fe + fo));
+      store_f(p, fma_(omf, f[p], fe - fo));
     }
   }
   st_pol(s.u + nu, u0, pol.once);
   st_pol(s.u + (Nu + nu), u1, pol.once);
   st_pol(s.u + (2 * Nu + nu), u2, pol.once);
-  st_pol(s.phi_out + nu, phi, pol.once);
+  if (STORE_PHI) st_pol(s.phi_out + nu, phi, pol.once);
+}
+
+// ---------------------------------------------------------------------------
+// Tile sums of phi.  Float phi in [0, 1] is summed as unsigned 64-bit fixed
+// point with 31 fraction bits: exact, so the total does not depend on the
+// order of summation or on the tiling, and free of the (slow on this part)
+// float64 pipe; NaN is carried by a flag.  Double phi is summed in double.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long kSumNaN = ~0ull;
+constexpr double kFix = 2147483648.0;  // 2^31
+
+template <typename T>
+struct TileSum {
+  double a = 0.0;
+  __device__ __forceinline__ void add(T phi) { a += (double)phi; }
+};
+template <>
+struct TileSum<float> {
+  unsigned long long a = 0ull;
+  bool nan = false;
+  __device__ __forceinline__ void add(float phi) {
+    a += (unsigned long long)__float2uint_rn(phi * 2147483648.0f);
+    nan |= !(phi == phi);
+  }
+};
+
+// Block total of the tile sums, published; the last block to finish adds the
+// block totals in block order and returns true in thread 0 with the grid
+// total in *total (NaN if any phi was NaN).  Resets the counter.
+template <typename T>
+__device__ __forceinline__ bool grid_phi_total(TileSum<T>& ts, double* partials, unsigned* counter,
+                                               double* total) {
+  if constexpr (sizeof(T) == 8) {
+    return last_block_total(block_sum(ts.a), partials, counter, total);
+  } else {
+    __shared__ unsigned long long s_warp[kBlock / 32];
+    __shared__ bool s_last;
+    unsigned long long v = ts.a;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const bool nan = __syncthreads_or(ts.nan) != 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) s_warp[wid] = v;
+    __syncthreads();
+    unsigned long long* up = reinterpret_cast<unsigned long long*>(partials);
+    if (threadIdx.x == 0) {
+      unsigned long long r = 0ull;
+#pragma unroll
+      for (int i = 0; i < kBlock / 32; ++i) r += s_warp[i];
+      up[blockIdx.x] = nan ? kSumNaN : r;
+      __threadfence();
+      s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    unsigned long long acc = 0ull;
+    bool any_nan = false;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+      const unsigned long long p = ((volatile unsigned long long*)up)[i];
+      if (p == kSumNaN) any_nan = true;
+      else acc += p;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    any_nan = __syncthreads_or(any_nan) != 0;
+    if (lane == 0) s_warp[wid] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long r = 0ull;
+#pragma unroll
+      for (int i = 0; i < kBlock / 32; ++i) r += s_warp[i];
+      *total = any_nan ? __longlong_as_double(0x7ff8000000000000ll) : (double)r / kFix;
+      *counter = 0u;
+    }
+    return threadIdx.x == 0;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -514,12 +707,27 @@ struct StepOccupancy {
   static constexpr int blocks = sizeof(T) == 8 ? 1 : (sizeof(S) == 2 ? 2 : 3);
 };
 
-template <typename T, typename S, bool RAW, bool FIRST>
+// Shared memory of the step kernel: phi and class of the halo tile, then (for
+// float and double populations) the staging slots, 16-byte aligned.
+template <typename T>
+__host__ __device__ __forceinline__ size_t stage_offset(const Tiling& tl) {
+  return ((size_t)tl.hmax * (sizeof(T) + 1) + 15) & ~(size_t)15;
+}
+template <typename T, typename S>
+size_t step_smem_bytes(const Tiling& tl) {
+  const bool staged = sizeof(S) == sizeof(T);
+  return stage_offset<T>(tl) + (staged ? (size_t)2 * kStage * kBlock * sizeof(T) : 0);
+}
+
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
 __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Consts<T> k, State<T, S> s, Tiling tl) {
   // shared memory: phi and node class of the tile and its halo
   extern __shared__ __align__(16) unsigned char smem[];
   T* sphi = reinterpret_cast<T*>(smem);
   uint8_t* scls = reinterpret_cast<uint8_t*>(sphi + tl.hmax);
+  // staging slots of phase B (float and double populations): 2 x kStage words per thread
+  constexpr bool STAGED = std::is_same<S, T>::value;
+  T* stage = reinterpret_cast<T*>(smem + stage_offset<T>(tl));
   const size_t N = (size_t)k.N;
   const Pol pol = Pol::make();
 
@@ -533,10 +741,28 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
   const int H = (ex_ + 2) * HY * HZ;
   const int E = ex_ * ey_ * ez_;
   const float inv_hz = 1.0f / (float)HZ, inv_hy = 1.0f / (float)HY;
+  const float inv_ez = 1.0f / (float)ez_, inv_ey = 1.0f / (float)ey_;
 
-  // phase A: phi on the tile and its halo; the tile's sum of phi accumulates in
-  // float64 so that it does not depend on the tiling
-  double part = 0.0;
+  // phase B's first chunk of g, u and previous phi does not depend on phi:
+  // its copies fly during phase A
+  auto stage_chunk = [&](int t, int slot) {
+    if constexpr (STAGED) {
+      if (t < E) {
+        const int r = fdiv(t, inv_ez);
+        const int lz = t - r * ez_;
+        const int lx = fdiv(r, inv_ey);
+        const int ly = r - lx * ey_;
+        const int n = ((x0 + lx) * k.ny + (y0 + ly)) * k.nz + (z0 + lz);
+        const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
+        stage_node<T, RAW, FIRST>(k, s, n, nb, stage + slot * kStage * kBlock + threadIdx.x, pol.once);
+      }
+      cp_async_commit();
+    }
+  };
+  stage_chunk(threadIdx.x, 0);
+
+  // phase A: phi on the tile and its halo, and the tile's sum of phi
+  TileSum<T> part;
   // no periodic wrap anywhere in the halo or its pull sources: constant offsets
   const bool inner = x0 >= 2 && x0 + ex_ + 2 <= k.nx && y0 >= 2 && y0 + ey_ + 2 <= k.ny && z0 >= 2 &&
                      z0 + ez_ + 2 <= k.nz;
@@ -563,7 +789,7 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
       }
       sphi[h] = phi;
       scls[h] = c;
-      if (own) part += (double)phi;
+      if (own) part.add(phi);
     }
   } else {
     for (int h = threadIdx.x; h < H; h += kBlock) {
@@ -588,19 +814,18 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
       }
       sphi[h] = phi;
       scls[h] = c;
-      if (own) part += (double)phi;
+      if (own) part.add(phi);
     }
   }
   __syncthreads();
 
-  // sum(phi) of the tile -> mass-correction factor of this step (:582-589)
-  part = block_sum(part);
+  // sum(phi) of the grid -> mass-correction factor of this step (:582-589)
   double total;
-  if (last_block_total(part, s.partials, s.counter, &total)) {
-    const T S = (T)total;
+  if (grid_phi_total<T>(part, s.partials, s.counter, &total)) {
+    const T sum = (T)total;
     T corr = T(1);
-    if (S > T(1e-6)) {
-      const T safe = S < T(1e-6) ? T(1e-6) : S;
+    if (sum > T(1e-6)) {
+      const T safe = sum < T(1e-6) ? T(1e-6) : sum;
       corr = (T(1) / safe) * (T)s.scal[0];
     } else {
       atomicOr(s.status, 2u);
@@ -610,31 +835,135 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
     s.scal[1] = total;
   }
 
-  // phase B: the tile's nodes
-  const float inv_ez = 1.0f / (float)ez_, inv_ey = 1.0f / (float)ey_;
+  // phase B: the tile's nodes, one chunk of kBlock nodes at a time; the next
+  // chunk's copies are started before this chunk is computed
   const int sx = HY * HZ;
-  for (int t = threadIdx.x; t < E; t += kBlock) {
-    const int r = fdiv(t, inv_ez);
-    const int lz = t - r * ez_;
-    const int lx = fdiv(r, inv_ey);
-    const int ly = r - lx * ey_;
-    const int h = ((lx + 1) * HY + (ly + 1)) * HZ + (lz + 1);
-    const int n = ((x0 + lx) * k.ny + (y0 + ly)) * k.nz + (z0 + lz);
-    const uint8_t c = scls[h];
-    const T phi = sphi[h];
-    T ps[Q];
-#pragma unroll
-    for (int q = 1; q < Q; ++q) ps[q] = sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)];
-    T gx, gy, gz, lap;
-    grad_lap<T, true>(k, s, n, c, phi, ps,
-                      [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; },
-                      gx, gy, gz, lap);
-    const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
-    // phi of this step at x + e_q: the next step's reader of slot (x, q) uses
-    // it as the deviation reference of the half form
-    collide_node<T, S, RAW, FIRST>(k, s, n, nb, c, phi, gx, gy, gz, lap, pol,
-                                   [&](int q) { return sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)]; });
+  const int nch = (E + kBlock - 1) / kBlock;
+  for (int j = 0; j < nch; ++j) {
+    const int t = j * kBlock + threadIdx.x;
+    if constexpr (STAGED) {
+      stage_chunk(t + kBlock, (j + 1) & 1);
+      cp_async_wait<1>();
+    }
+    if (t < E) {
+      const int r = fdiv(t, inv_ez);
+      const int lz = t - r * ez_;
+      const int lx = fdiv(r, inv_ey);
+      const int ly = r - lx * ey_;
+      const int h = ((lx + 1) * HY + (ly + 1)) * HZ + (lz + 1);
+      const int n = ((x0 + lx) * k.ny + (y0 + ly)) * k.nz + (z0 + lz);
+      const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
+      // phi of this step at x + e_q (also the deviation reference, in the half
+      // form, of the next step's reader of slot (x, q))
+      update_node<T, S, RAW, FIRST, OMEGA1, STAGED, true>(
+          k, s, n, nb, scls[h], sphi[h], [&](int q) { return sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)]; },
+          [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; }, pol,
+          stage + (j & 1) * kStage * kBlock + threadIdx.x);
+    }
   }
+  if constexpr (STAGED) cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// The two-kernel time step: k_phi recovers phi of every node (one thread per
+// node, linear order) and the grid sum of phi; k_update then runs the rest of
+// the step for every node, reading the phi stencil from L2.  Both stream their
+// arrays in z-fastest order, so warps move whole 128-byte lines.  With
+// omega_f == 1 f is read by k_phi only, and the pair moves the algorithmic
+// bytes of the step plus the phi stencil's L2 traffic.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void decode(const FastDiv& dz, const FastDiv& dy, int n, int nz, int ny, int& ix,
+                                       int& iy, int& iz) {
+  const int t = (int)dz.div((unsigned)n);
+  iz = n - t * nz;
+  ix = (int)dy.div((unsigned)t);
+  iy = t - ix * ny;
+}
+
+// Persistent: a grid of about one wave strides over the nodes, so that the
+// per-block publication of the partial sum happens once per block.
+template <typename T, typename S, bool RAW>
+__global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
+  const Pol pol = Pol::make();
+  TileSum<T> part;
+  for (int n = blockIdx.x * kBlock + threadIdx.x; n < k.N; n += gridDim.x * kBlock) {
+    const uint8_t c = s.cls[n];
+    T phi = T(0);
+    if (!(c & kSolid)) {
+      int ix, iy, iz;
+      decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
+      const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
+      const T eps = (c & kPartial) ? s.eps[n] : T(0);
+      T v[Q];
+      // f is read again by k_update only when omega_f != 1
+      fetch_f<T, S, RAW, true>(v, k, s, n, (size_t)k.N, nb, c, eps, k.omega_f == T(1) ? pol.once : pol.keep);
+      phi = clamp01(seqsum(v));
+    }
+    st_pol(s.phi_out + n, phi, pol.keep);  // read back (stencil) by k_update
+    part.add(phi);
+  }
+  // sum(phi) of the grid -> mass-correction factor of this step (:582-589)
+  double total;
+  if (grid_phi_total<T>(part, s.partials, s.counter, &total)) {
+    const T sum = (T)total;
+    T corr = T(1);
+    if (sum > T(1e-6)) {
+      const T safe = sum < T(1e-6) ? T(1e-6) : sum;
+      corr = (T(1) / safe) * (T)s.scal[0];
+    } else {
+      atomicOr(s.status, 2u);
+    }
+    if (!(total == total) || total - total != 0.0) atomicOr(s.status, 1u);
+    s.cbuf[s.c_cur] = corr;
+    s.scal[1] = total;
+  }
+}
+
+template <typename T, typename S>
+struct UpdateOccupancy {
+  static constexpr int blocks = sizeof(T) == 8 ? 1 : (sizeof(S) == 2 ? 2 : 3);
+};
+
+// One thread per node, linear order.  (A persistent form that stages the next
+// node's g, u and previous phi in shared memory with cp.async measured slower:
+// the copies and the smaller L1 cost more than the latency they hide.)
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
+__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_update(Consts<T> k, State<T, S> s) {
+  const Pol pol = Pol::make();
+  const int n = blockIdx.x * kBlock + threadIdx.x;
+  if (n >= k.N) return;
+  int ix, iy, iz;
+  decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
+  const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
+  const T* __restrict__ pc = s.phi_out;  // phi of this step (k_phi)
+  const uint8_t c = s.cls[n];
+  const T phi = ld_pol(pc + n, pol.keep);
+  update_node<T, S, RAW, FIRST, OMEGA1, false, false>(
+      k, s, n, nb, c, phi, [&](int q) { return ld_pol(pc + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); },
+      [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; }, pol, (const T*)nullptr);
+}
+
+// Grid of the persistent k_phi: resident blocks per SM x SMs (about one wave),
+// at most one block per kBlock nodes.
+template <typename T, typename S, bool RAW>
+static cudaError_t phi_grid(const Consts<T>& k, int* grid) {
+  // one lookup per instantiation and device
+  static int cached_dev = -1, cached = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (cached_dev != dev) {
+    int nsm = 0, b = 0;
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_phi<T, S, RAW>, kBlock, 0);
+    if (e != cudaSuccess) return e;
+    cached = nsm * (b > 0 ? b : 1);
+    cached_dev = dev;
+  }
+  const int full = (k.N + kBlock - 1) / kBlock;
+  *grid = cached < full ? cached : full;
+  return cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------
@@ -657,12 +986,12 @@ __global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T, S> s, con
     for (int q = 0; q < Q; ++q) {
       const T ec = edot(q, v0, v1, v2) / k.cs2;
       // the state right after init is read in place (RAW): deviation reference = own phi
-      f[(size_t)q * N + n] = IO::st_f(phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b)), q, phi, k);
-      g[(size_t)q * N + n] = IO::st_g(T(0) * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b), q, k);
+      f[(size_t)q * k.Np + n] = IO::st_f(phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b)), q, phi, k);
+      g[(size_t)q * k.Np + n] = IO::st_g(T(0) * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b), q, k);
     }
     s.u[n] = v0;
-    s.u[N + n] = v1;
-    s.u[2 * N + n] = v2;
+    s.u[k.Np + n] = v1;
+    s.u[2 * (size_t)k.Np + n] = v2;
     s.phi_out[n] = phi;
     part = (double)phi;
   }
@@ -706,8 +1035,8 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
   if (mask & 2u) rho_o[n] = rho;
   if (mask & 4u) {
     u_o[n] = s.u[n];
-    u_o[N + n] = s.u[N + n];
-    u_o[2 * N + n] = s.u[2 * N + n];
+    u_o[N + n] = s.u[k.Np + n];
+    u_o[2 * N + n] = s.u[2 * (size_t)k.Np + n];
   }
   if (mask & (8u | 16u | 32u)) {
     int ix, iy, iz;
@@ -868,15 +1197,10 @@ __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, cons
 // ---------------------------------------------------------------------------
 // Host-side launchers (called from lbm_capi.cu)
 // ---------------------------------------------------------------------------
-template <typename T>
-size_t step_smem_bytes(const Tiling& tl) {
-  return (size_t)tl.hmax * (sizeof(T) + 1);
-}
-
-template <typename T, typename S, bool RAW, bool FIRST>
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
 static cudaError_t launch_step_t(const Consts<T>& k, const State<T, S>& s, const Tiling& tl, cudaStream_t st) {
-  const size_t sm = step_smem_bytes<T>(tl);
-  auto fn = k_step<T, S, RAW, FIRST>;
+  const size_t sm = step_smem_bytes<T, S>(tl);
+  auto fn = k_step<T, S, RAW, FIRST, OMEGA1>;
   if (sm > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
@@ -885,13 +1209,34 @@ static cudaError_t launch_step_t(const Consts<T>& k, const State<T, S>& s, const
   return cudaGetLastError();
 }
 
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
+static cudaError_t launch_two_t(const Consts<T>& k, const State<T, S>& s, cudaStream_t st) {
+  int gphi = 0;
+  cudaError_t e = phi_grid<T, S, RAW>(k, &gphi);
+  if (e != cudaSuccess) return e;
+  k_phi<T, S, RAW><<<gphi, kBlock, 0, st>>>(k, s);
+  k_update<T, S, RAW, FIRST, OMEGA1><<<(k.N + kBlock - 1) / kBlock, kBlock, 0, st>>>(k, s);
+  return cudaGetLastError();
+}
+
+// The first step after init reads the reference state in place (RAW) and has
+// no phi u of a previous step (FIRST); every later step is neither.  A tiling
+// with tx == 0 selects the two-kernel step, else the fused tiled kernel.
 template <typename T, typename S>
 cudaError_t launch_step(const Consts<T>& k, const State<T, S>& s, const Tiling& tl, bool raw, bool first,
                         cudaStream_t st) {
-  if (raw && first) return launch_step_t<T, S, true, true>(k, s, tl, st);
-  if (raw) return launch_step_t<T, S, true, false>(k, s, tl, st);
-  if (first) return launch_step_t<T, S, false, true>(k, s, tl, st);
-  return launch_step_t<T, S, false, false>(k, s, tl, st);
+  if (raw != first) return cudaErrorInvalidValue;
+  if (tl.tx == 0) {
+    const bool om1 = k.omega_f == T(1);
+    if (raw)
+      return om1 ? launch_two_t<T, S, true, true, true>(k, s, st) : launch_two_t<T, S, true, true, false>(k, s, st);
+    return om1 ? launch_two_t<T, S, false, false, true>(k, s, st) : launch_two_t<T, S, false, false, false>(k, s, st);
+  }
+  const bool om1 = k.omega_f == T(1);
+  if (raw)
+    return om1 ? launch_step_t<T, S, true, true, true>(k, s, tl, st) : launch_step_t<T, S, true, true, false>(k, s, tl, st);
+  return om1 ? launch_step_t<T, S, false, false, true>(k, s, tl, st)
+             : launch_step_t<T, S, false, false, false>(k, s, tl, st);
 }
 
 template <typename T, typename S, typename Src>
@@ -994,8 +1339,9 @@ template cudaError_t launch_measure_static<float>(int, int, int, const float*, c
 template cudaError_t launch_measure_static<double>(int, int, int, const double*, const uint8_t*, double*,
                                                    cudaStream_t);
 
-template size_t step_smem_bytes<float>(const Tiling&);
-template size_t step_smem_bytes<double>(const Tiling&);
+template size_t step_smem_bytes<float, float>(const Tiling&);
+template size_t step_smem_bytes<double, double>(const Tiling&);
+template size_t step_smem_bytes<float, __half>(const Tiling&);
 
 #define LBM_INSTANTIATE(T, S)                                                                                   \
   template cudaError_t launch_step<T, S>(const Consts<T>&, const State<T, S>&, const Tiling&, bool, bool,        \
