@@ -42,13 +42,17 @@ import numpy as np  # noqa: E402
 
 # Algorithmic bytes per node and step, float32 state: f and g (2 x 19
 # populations), u (3) and the previous phi (1), each read once and written
-# once: 2 x 4 x (38 + 3 + 1) = 336 B.
-B_ALG_STEP = 336
-# The fused step kernel k_step moves those 336 B plus the node-class byte.
-B_ALG_KERNEL = 337
-# Half-precision population storage: 2 x 2 x 38 + 2 x 4 x 4 = 184 B (+1).
-B_ALG_STEP_F16 = 184
-B_ALG_KERNEL_F16 = 185
+# once: 2 x 4 x (38 + 3 + 1) = 336 B.  Half-precision population storage:
+# 2 x 2 x 38 + 2 x 4 x 4 = 184 B.
+B_ALG_STEP = {"fp32": 336, "fp16": 184}
+# Per kernel (each adds the node-class byte it reads):
+#   k_phi     f read (76 | 38), phi written (4), in the half form also the
+#             previous phi (4, the deviation reference)
+#   k_update  g (76 | 38), u (12) and previous phi (4) read; f, g (76 + 76 |
+#             38 + 38) and u (12) written; the phi stencil comes from L2
+#   k_step    the fused kernel: the whole step
+B_ALG_KERNEL = {"fp32": {"k_phi": 81, "k_update": 257, "k_step": 337},
+                "fp16": {"k_phi": 47, "k_update": 143, "k_step": 185}}
 
 WORKLOADS = {
     "ridge150": dict(grid=(150, 150, 107), substrate=("ridge", 1.0, 22.5), center=(75, 75, 80),
@@ -240,7 +244,8 @@ def run_ours(args, rank, world, device):
         torch.cuda.synchronize(device)
     barrier(world)
     s.step_count += K
-    ker_ms, tot_ms = float(ms3[1]), float(ms3[2])
+    phi_ms, upd_ms, tot_ms = float(ms3[0]), float(ms3[1]), float(ms3[2])
+    two_kernel = tuple(s.get_tile()) == (0, 0, 0)
     tot_ms = max_over_ranks(tot_ms, world, device)
     status = s.status()
     meas = s.measure()
@@ -273,12 +278,21 @@ def run_ours(args, rank, world, device):
     if rank == 0:
         peak, peak_kind = peaks()
         f16 = args.precision == "fp16"
-        b_ker = B_ALG_KERNEL_F16 if f16 else B_ALG_KERNEL
-        b_step = B_ALG_STEP_F16 if f16 else B_ALG_STEP
-        ker_s = ker_ms / K / 1e3
+        b_step = B_ALG_STEP[args.precision]
+        # the dominant kernel of the step: k_update (two-kernel step) or k_step (fused)
+        kname = "k_update" if two_kernel else "k_step"
+        b_ker = B_ALG_KERNEL[args.precision][kname]
+        ker_s = upd_ms / K / 1e3
         achieved = b_ker * n / ker_s / 1e9
-        traffic_pn = profiled_traffic("k_step_f16" if f16 else "k_step")
+        traffic_pn = profiled_traffic(kname + ("_f16" if f16 else ""))
         step_bw = b_step * n / (tot_ms / K / 1e3) / 1e9
+        kernels = {}
+        if two_kernel:
+            b_phi = B_ALG_KERNEL[args.precision]["k_phi"]
+            kernels = {"k_phi": {"ms_per_launch": phi_ms / K, "bytes_per_node": b_phi,
+                                 "achieved_gbs": b_phi * n / (phi_ms / K / 1e3) / 1e9},
+                       "k_update": {"ms_per_launch": upd_ms / K, "bytes_per_node": b_ker,
+                                    "achieved_gbs": achieved}}
         w = WORKLOADS[name]
         cpu = None
         if not args.no_cpu_baseline:
@@ -303,11 +317,12 @@ def run_ours(args, rank, world, device):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic_pn * n if traffic_pn is not None else None,
-                         "kernel": "k_step", "bytes_per_node": b_ker,
-                         "ms_per_launch": ker_ms / K},
+                         "kernel": kname, "bytes_per_node": b_ker,
+                         "ms_per_launch": upd_ms / K},
             "step_roofline": {"achieved_gbs": step_bw, "bytes_per_node": b_step, "peak": peak,
                               "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / b_step},
-            "gpu_launches": K,
+            "kernels": kernels,
+            "gpu_launches": 2 * K if two_kernel else K,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "spread_after": {k2: meas[k2] for k2 in ("Dx", "Dy", "k", "z_com", "volume")},

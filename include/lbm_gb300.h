@@ -115,10 +115,12 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
  * (lbm/fe_ac_solver.py:380-639).  Asynchronous on `stream`; no host sync. */
 int lbm_step(LbmHandle* h, int nsteps, void* stream);
 
-/* As lbm_step, with CUDA events recorded on `stream` around the step kernel
- * launches; on return (synchronised) kernel_ms3[1] holds their summed
- * duration, kernel_ms3[2] the whole span and kernel_ms3[0] zero.  For
- * measurement; same results as lbm_step. */
+/* As lbm_step, with CUDA events recorded on `stream` before each step, between
+ * its two kernels (before the fused kernel) and after the last step; on return
+ * (synchronised) kernel_ms3[0] holds the summed duration of the phi kernels
+ * (zero for the fused kernel), kernel_ms3[1] that of the update (or fused)
+ * kernels and kernel_ms3[2] the whole span.  For measurement; same results as
+ * lbm_step. */
 int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3);
 
 /* Step kernel selection.  (0, 0, 0), the default, selects the two-kernel

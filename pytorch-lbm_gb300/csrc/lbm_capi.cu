@@ -20,7 +20,8 @@ namespace lbm {
 template <typename T, typename S>
 size_t step_smem_bytes(const Tiling&);
 template <typename T, typename S>
-cudaError_t launch_step(const Consts<T>&, const State<T, S>&, const Tiling&, bool, bool, cudaStream_t);
+cudaError_t launch_step(const Consts<T>&, const State<T, S>&, const Tiling&, bool, bool, cudaStream_t,
+                        cudaEvent_t = nullptr);
 template <typename T, typename S, typename Src>
 cudaError_t launch_init(const Consts<T>&, const State<T, S>&, const Src*, const Src*, cudaStream_t);
 template <typename T, typename S>
@@ -286,8 +287,8 @@ int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr
     State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
     s.c_prev = h->c_last;
     s.c_cur = h->c_last ^ 1;
-    if (ev) CUDA_TRY(cudaEventRecord(ev[i], st));
-    CUDA_TRY(launch_step<T>(k, s, h->tiling, h->raw, h->first, st));
+    if (ev) CUDA_TRY(cudaEventRecord(ev[2 * i], st));
+    CUDA_TRY(launch_step<T>(k, s, h->tiling, h->raw, h->first, st, ev ? ev[2 * i + 1] : nullptr));
     h->last_raw_in = h->raw;
     h->cur ^= 1;
     h->pc ^= 1;
@@ -296,7 +297,7 @@ int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr
     h->first = false;
     ++h->steps;
   }
-  if (ev) CUDA_TRY(cudaEventRecord(ev[nsteps], st));
+  if (ev) CUDA_TRY(cudaEventRecord(ev[2 * nsteps], st));
   return LBM_OK;
 }
 
@@ -370,10 +371,10 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
     A(&h->g[b], (size_t)Q * Np * h->psize);
   }
   A(&h->u, 3 * Np * T);
-  A(&h->phi[0], N * T);
-  A(&h->phi[1], N * T);
+  A(&h->phi[0], Np * T);  // phi and class arrays padded to Np like the populations
+  A(&h->phi[1], Np * T);
   A(&h->eps, N * T);
-  A((void**)&h->cls, N);
+  A((void**)&h->cls, Np);
   A((void**)&h->wn, 3 * N * sizeof(float));
   A((void**)&h->partials, npart * sizeof(double));
   A((void**)&h->counters, 4 * sizeof(unsigned));
@@ -381,6 +382,9 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   A((void**)&h->scal, 16 * sizeof(double));
   A(&h->meas_phi, N * T);
   if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(h->phi[0], 0, Np * T);
+  if (e == cudaSuccess) e = cudaMemset(h->phi[1], 0, Np * T);
+  if (e == cudaSuccess) e = cudaMemset(h->cls, 0, Np);
   if (e == cudaSuccess) e = cudaMemset(h->scal, 0, 16 * sizeof(double));
   if (e != cudaSuccess) {
     free_all(h);
@@ -478,20 +482,29 @@ int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3)
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_step_profiled: call lbm_init_fields first");
   if (nsteps <= 0) return fail(LBM_E_ARG, "lbm_step_profiled: nsteps must be positive");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  std::vector<cudaEvent_t> ev((size_t)nsteps + 1, nullptr);
+  // events: before each step, between its phi and update kernels (before the
+  // fused kernel), and after the last step
+  std::vector<cudaEvent_t> ev(2 * (size_t)nsteps + 1, nullptr);
   for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
   int rc = with_types(h->prec, [&](auto tag) {
     return do_step<typename decltype(tag)::T, typename decltype(tag)::S>(h, nsteps, st, ev.data());
   });
-  float tot = 0.f;
+  float tot = 0.f, a = 0.f, b = 0.f;
   if (rc == LBM_OK) {
     cudaError_t e = cudaEventSynchronize(ev.back());
     if (e == cudaSuccess) e = cudaEventElapsedTime(&tot, ev.front(), ev.back());
+    for (int i = 0; i < nsteps && e == cudaSuccess; ++i) {
+      float x = 0.f, y = 0.f;
+      e = cudaEventElapsedTime(&x, ev[2 * i], ev[2 * i + 1]);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&y, ev[2 * i + 1], ev[2 * i + 2]);
+      a += x;
+      b += y;
+    }
     if (e != cudaSuccess) rc = fail(LBM_E_CUDA, std::string("lbm_step_profiled: ") + cudaGetErrorString(e));
   }
   for (auto& e : ev) cudaEventDestroy(e);
-  kernel_ms3[0] = 0.f;
-  kernel_ms3[1] = tot;
+  kernel_ms3[0] = a;
+  kernel_ms3[1] = b;
   kernel_ms3[2] = tot;
   return rc;
 }

@@ -292,7 +292,12 @@ __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const Sta
 // (lbm/fe_ac_solver.py:296-320 fused, :282-294 unfused; fe_wetting.py:418-446).
 // ps[q] holds phi(x + e_q); nsolid(q) tells whether that neighbour is solid.
 // ---------------------------------------------------------------------------
-template <typename T, bool FUSED, typename St, typename SolidFn>
+// PAIR: the gradient from opposite-pair differences t_q = (w_q / cs2)
+// (phi(x + e_q) - phi(x - e_q)), nine products instead of thirty, with
+// mirror partners summed first so that a mirror-symmetric phi still gives
+// an exactly zero component (the sharpening normal grad / |grad| depends on
+// it where the gradient vanishes).
+template <typename T, bool FUSED, typename St, typename SolidFn, bool PAIR = false>
 __device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n, uint8_t c, T phi,
                                          T (&ps)[Q], SolidFn nsolid, T& gx, T& gy, T& gz, T& lap) {
   if (k.wetting && (c & kBoundary)) {
@@ -314,11 +319,21 @@ __device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n,
     }
   }
   gx = gy = gz = lap = T(0);
+  if constexpr (PAIR) {
+    auto t = [&](int q) { return mul_rn(k.wc[q], ps[q] - ps[opp(q)]); };
+    const T t1 = t(1), t3 = t(3), t5 = t(5), t7 = t(7), t8 = t(8), t11 = t(11), t12 = t(12), t15 = t(15),
+            t16 = t(16);
+    gx = add_rn(add_rn(t1, t7 - t8), t11 - t12);  // e_x: q 1, 7, -8, 11, -12 (and their opposites)
+    gy = add_rn(add_rn(t3, t7 + t8), t15 - t16);  // e_y: q 3, 7, 8, 15, -16
+    gz = add_rn(add_rn(t5, t11 + t12), t15 + t16);  // e_z: q 5, 11, 12, 15, 16
+  }
 #pragma unroll
   for (int q = 1; q < Q; ++q) {
-    if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
-    if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
-    if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
+    if (!PAIR) {
+      if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
+      if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
+      if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
+    }
     if (FUSED) {
       lap = lap + k.w2c[q] * (ps[q] - phi);
     } else {
@@ -391,8 +406,8 @@ __device__ __forceinline__ void stage_node(const Consts<T>& k, const State<T, T>
   if (!FIRST) cp_async(st + (Q + 3) * kBlock, s.phi_in + nu, pol);
 }
 
-// STAGED: g, u and the previous phi come from the node's staging slot `st`
-// (float and double populations); otherwise they are loaded here.
+// STAGED: g, u and the previous phi come from the node's cp.async staging
+// slot `st` (word j at st[j * kBlock]); otherwise they are loaded here.
 template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool STAGED, bool STORE_PHI, typename PhiAt,
           typename SolidAt>
 __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S>& s, int n, const Nbr& nb,
@@ -439,7 +454,7 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
 #pragma unroll
   for (int q = 1; q < Q; ++q) ps[q] = phi_at(q);
   T gx, gy, gz, lap;
-  grad_lap<T, true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
+  grad_lap<T, true, State<T, S>, SolidAt, true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
 
   const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
@@ -469,33 +484,31 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     }
   }
 
-  // 3. pressure from the hydrodynamic populations
-  const T P = seqsum(g);
-
-  // 4. non-equilibrium stress with the new P and the old u (:409-413):
-  // sum_q e_a e_b (g_q - g_eq_q) = Pi_ab - P cs2 delta_ab - u_a u_b, since the
-  // D3Q19 weights satisfy sum w e_a e_b = cs2 delta_ab and
+  // 3.-4. moments of g from opposite-pair sums s_i = g_q + g_opp q and
+  // differences d_i = g_q - g_opp q (pairs i = 0..8: q = 1, 3, 5, 7, 8, 11,
+  // 12, 15, 16): pressure P = sum g, momentum sum e g, and the second moment
+  // Pi = sum e e g, from which the non-equilibrium stress with the new P and
+  // the old u (:409-413) is Pi_ab - P cs2 delta_ab - u_a u_b, since the D3Q19
+  // weights satisfy sum w e_a e_b = cs2 delta_ab and
   // sum w e_a e_b e_c e_d = cs2^2 (delta_ab delta_cd + delta_ac delta_bd + delta_ad delta_bc).
+  T sp[9], dp[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    sp[i] = g[pair_first(i)] + g[opp(pair_first(i))];
+    dp[i] = g[pair_first(i)] - g[opp(pair_first(i))];
+  }
+  T P = g[0];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) P = P + sp[i];
   T sxx, syy, szz, sxy, sxz, syz;
   {
-    bool fxx = true, fyy = true, fzz = true, fxy = true, fxz = true, fyz = true;
-    sxx = syy = szz = sxy = sxz = syz = T(0);
-#pragma unroll
-    for (int q = 1; q < Q; ++q) {
-      if (ex(q) != 0) { sxx = fxx ? g[q] : sxx + g[q]; fxx = false; }
-      if (ey(q) != 0) { syy = fyy ? g[q] : syy + g[q]; fyy = false; }
-      if (ez(q) != 0) { szz = fzz ? g[q] : szz + g[q]; fzz = false; }
-      if (ex(q) * ey(q) != 0) { const T t = ex(q) * ey(q) > 0 ? g[q] : -g[q]; sxy = fxy ? t : sxy + t; fxy = false; }
-      if (ex(q) * ez(q) != 0) { const T t = ex(q) * ez(q) > 0 ? g[q] : -g[q]; sxz = fxz ? t : sxz + t; fxz = false; }
-      if (ey(q) * ez(q) != 0) { const T t = ey(q) * ez(q) > 0 ? g[q] : -g[q]; syz = fyz ? t : syz + t; fyz = false; }
-    }
     const T pc = P * k.cs2;
-    sxx = (sxx - pc) - uo0 * uo0;
-    syy = (syy - pc) - uo1 * uo1;
-    szz = (szz - pc) - uo2 * uo2;
-    sxy = sxy - uo0 * uo1;
-    sxz = sxz - uo0 * uo2;
-    syz = syz - uo1 * uo2;
+    sxx = ((sp[0] + (sp[3] + sp[4]) + (sp[5] + sp[6])) - pc) - uo0 * uo0;
+    syy = ((sp[1] + (sp[3] + sp[4]) + (sp[7] + sp[8])) - pc) - uo1 * uo1;
+    szz = ((sp[2] + (sp[5] + sp[6]) + (sp[7] + sp[8])) - pc) - uo2 * uo2;
+    sxy = (sp[3] - sp[4]) - uo0 * uo1;
+    sxz = (sp[5] - sp[6]) - uo0 * uo2;
+    syz = (sp[7] - sp[8]) - uo1 * uo2;
   }
 
   // 5. forces (Fakhari 2017, :416-439)
@@ -520,18 +533,10 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   // 6. velocity (:442-447)
   T u0, u1, u2;
   {
-    bool f0 = true, f1 = true, f2 = true;
-    u0 = u1 = u2 = T(0);
-#pragma unroll
-    for (int q = 1; q < Q; ++q) {
-      if (ex(q) != 0) { const T t = ex(q) > 0 ? g[q] : -g[q]; u0 = f0 ? t : u0 + t; f0 = false; }
-      if (ey(q) != 0) { const T t = ey(q) > 0 ? g[q] : -g[q]; u1 = f1 ? t : u1 + t; f1 = false; }
-      if (ez(q) != 0) { const T t = ez(q) > 0 ? g[q] : -g[q]; u2 = f2 ? t : u2 + t; f2 = false; }
-    }
     const T hr = T(0.5) * rcp(rho_eff);
-    u0 = u0 + F0 * hr;
-    u1 = u1 + F1 * hr;
-    u2 = u2 + F2 * hr;
+    u0 = (dp[0] + (dp[3] - dp[4]) + (dp[5] - dp[6])) + F0 * hr;
+    u1 = (dp[1] + (dp[3] + dp[4]) + (dp[7] - dp[8])) + F1 * hr;
+    u2 = (dp[2] + (dp[5] + dp[6]) + (dp[7] + dp[8])) + F2 * hr;
     if (c & kSolid) u0 = u1 = u2 = T(0);
   }
   const T b = ((u0 * u0 + u1 * u1) + u2 * u2) * k.inv_two_cs2;
@@ -588,21 +593,30 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     const T f0 = pw * omb;
     store_f(0, OMEGA1 ? f0 : fma_(T(1) - k.omega_f, f[0], f0));
   }
+  // per weight class (axis pairs i < 3, diagonal pairs i >= 3): omega w,
+  // omega w / 2, omega w (P - b), nsd w; omega_f phi w, its half, omega_f phi w (1 - b)
+  const T wa = k.w[1], wd = k.w[7];
+  const T owa = om * wa, owd = om * wd;
+  const T howa = T(0.5) * owa, howd = T(0.5) * owd;
+  const T obpa = owa * Pb, obpd = owd * Pb;
+  const T nwa = nsd * wa, nwd = nsd * wd;
+  const T pwa = pf * wa, pwd = pf * wd;
+  const T hpwa = T(0.5) * pwa, hpwd = T(0.5) * pwd;
+  const T pwba = pwa * omb, pwbd = pwd * omb;
+  const T aca = k.wac3[1], acd = k.wac3[7];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
     const int q = pair_first(i), p = opp(q);
-    const T wq = k.w[q];
+    const bool ax = i < 3;
     const T ec = edot(q, u3x, u3y, u3z);
     // hydrodynamic pair
-    const T ow = om * wq;
-    const T ge = fma_((T(0.5) * ow) * ec, ec, ow * Pb);
-    const T go = fma_(ow, ec, (nsd * wq) * edot(q, F0, F1, F2));
+    const T ge = fma_((ax ? howa : howd) * ec, ec, ax ? obpa : obpd);
+    const T go = fma_(ax ? owa : owd, ec, (ax ? nwa : nwd) * edot(q, F0, F1, F2));
     store_g(q, fma_(omo, g[q], ge + go));
     store_g(p, fma_(omo, g[p], ge - go));
     // phase-field pair
-    const T pw = pf * wq;
-    const T fe = fma_((T(0.5) * pw) * ec, ec, pw * omb);
-    const T fo = fma_(pw, ec, k.wac3[q] * edot(q, S0, S1, S2));
+    const T fe = fma_((ax ? hpwa : hpwd) * ec, ec, ax ? pwba : pwbd);
+    const T fo = fma_(ax ? pwa : pwd, ec, (ax ? aca : acd) * edot(q, S0, S1, S2));
     if (OMEGA1) {
       store_f(q, fe + fo);
       store_f(p, fe - fo);
@@ -921,17 +935,11 @@ __global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
 
 template <typename T, typename S>
 struct UpdateOccupancy {
-  static constexpr int blocks = sizeof(T) == 8 ? 1 : (sizeof(S) == 2 ? 2 : 3);
+  static constexpr int blocks = sizeof(T) == 8 ? 1 : (sizeof(S) == 2 ? 3 : 4);
 };
 
-// One thread per node, linear order.  (A persistent form that stages the next
-// node's g, u and previous phi in shared memory with cp.async measured slower:
-// the copies and the smaller L1 cost more than the latency they hide.)
 template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
-__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_update(Consts<T> k, State<T, S> s) {
-  const Pol pol = Pol::make();
-  const int n = blockIdx.x * kBlock + threadIdx.x;
-  if (n >= k.N) return;
+__device__ __forceinline__ void update_one(const Consts<T>& k, const State<T, S>& s, int n, const Pol& pol) {
   int ix, iy, iz;
   decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
   const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
@@ -943,11 +951,22 @@ __global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_updat
       [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; }, pol, (const T*)nullptr);
 }
 
-// Grid of the persistent k_phi: resident blocks per SM x SMs (about one wave),
-// at most one block per kBlock nodes.
-template <typename T, typename S, bool RAW>
-static cudaError_t phi_grid(const Consts<T>& k, int* grid) {
-  // one lookup per instantiation and device
+// One thread per node, linear order.  (Measured slower on the 150x150x107
+// case: a persistent grid-stride form, and forms that stage the next node's
+// g, u and previous phi in shared memory with cp.async or with bulk copies
+// per chunk of nodes -- the copies, the smaller L1 and the block-wide waits
+// cost more than the latency they hide.)
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
+__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_update(Consts<T> k, State<T, S> s) {
+  const int n = blockIdx.x * kBlock + threadIdx.x;
+  if (n < k.N) update_one<T, S, RAW, FIRST, OMEGA1>(k, s, n, Pol::make());
+}
+
+// Grid of a persistent kernel: resident blocks per SM x SMs (one wave), at
+// most one block per kBlock nodes.  The occupancy lookup runs once per kernel
+// and device.
+template <typename Kern>
+static cudaError_t resident_grid(Kern fn, int nodes, int* grid) {
   static int cached_dev = -1, cached = 0;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -956,12 +975,12 @@ static cudaError_t phi_grid(const Consts<T>& k, int* grid) {
     int nsm = 0, b = 0;
     e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_phi<T, S, RAW>, kBlock, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, kBlock, 0);
     if (e != cudaSuccess) return e;
     cached = nsm * (b > 0 ? b : 1);
     cached_dev = dev;
   }
-  const int full = (k.N + kBlock - 1) / kBlock;
+  const int full = (nodes + kBlock - 1) / kBlock;
   *grid = cached < full ? cached : full;
   return cudaSuccess;
 }
@@ -1210,11 +1229,15 @@ static cudaError_t launch_step_t(const Consts<T>& k, const State<T, S>& s, const
 }
 
 template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
-static cudaError_t launch_two_t(const Consts<T>& k, const State<T, S>& s, cudaStream_t st) {
+static cudaError_t launch_two_t(const Consts<T>& k, const State<T, S>& s, cudaStream_t st, cudaEvent_t mid) {
   int gphi = 0;
-  cudaError_t e = phi_grid<T, S, RAW>(k, &gphi);
+  cudaError_t e = resident_grid(k_phi<T, S, RAW>, k.N, &gphi);
   if (e != cudaSuccess) return e;
   k_phi<T, S, RAW><<<gphi, kBlock, 0, st>>>(k, s);
+  if (mid) {
+    e = cudaEventRecord(mid, st);
+    if (e != cudaSuccess) return e;
+  }
   k_update<T, S, RAW, FIRST, OMEGA1><<<(k.N + kBlock - 1) / kBlock, kBlock, 0, st>>>(k, s);
   return cudaGetLastError();
 }
@@ -1222,15 +1245,23 @@ static cudaError_t launch_two_t(const Consts<T>& k, const State<T, S>& s, cudaSt
 // The first step after init reads the reference state in place (RAW) and has
 // no phi u of a previous step (FIRST); every later step is neither.  A tiling
 // with tx == 0 selects the two-kernel step, else the fused tiled kernel.
+// `mid` (may be null) is recorded between k_phi and k_update, or before the
+// fused kernel.
 template <typename T, typename S>
 cudaError_t launch_step(const Consts<T>& k, const State<T, S>& s, const Tiling& tl, bool raw, bool first,
-                        cudaStream_t st) {
+                        cudaStream_t st, cudaEvent_t mid) {
   if (raw != first) return cudaErrorInvalidValue;
   if (tl.tx == 0) {
     const bool om1 = k.omega_f == T(1);
     if (raw)
-      return om1 ? launch_two_t<T, S, true, true, true>(k, s, st) : launch_two_t<T, S, true, true, false>(k, s, st);
-    return om1 ? launch_two_t<T, S, false, false, true>(k, s, st) : launch_two_t<T, S, false, false, false>(k, s, st);
+      return om1 ? launch_two_t<T, S, true, true, true>(k, s, st, mid)
+                 : launch_two_t<T, S, true, true, false>(k, s, st, mid);
+    return om1 ? launch_two_t<T, S, false, false, true>(k, s, st, mid)
+               : launch_two_t<T, S, false, false, false>(k, s, st, mid);
+  }
+  if (mid) {
+    cudaError_t e = cudaEventRecord(mid, st);
+    if (e != cudaSuccess) return e;
   }
   const bool om1 = k.omega_f == T(1);
   if (raw)
@@ -1345,7 +1376,7 @@ template size_t step_smem_bytes<float, __half>(const Tiling&);
 
 #define LBM_INSTANTIATE(T, S)                                                                                   \
   template cudaError_t launch_step<T, S>(const Consts<T>&, const State<T, S>&, const Tiling&, bool, bool,        \
-                                         cudaStream_t);                                                          \
+                                         cudaStream_t, cudaEvent_t);                                             \
   template cudaError_t launch_init<T, S, float>(const Consts<T>&, const State<T, S>&, const float*, const float*,  \
                                                 cudaStream_t);                                                   \
   template cudaError_t launch_init<T, S, double>(const Consts<T>&, const State<T, S>&, const double*,             \

@@ -368,8 +368,9 @@ class AllenCahnSolver:
         return d
 
     def autotune(self, reps=5, stream=None):
-        """Pick the fastest tile shape of the step kernel on the current state
-        (the state is left unchanged).  Returns ((tx, ty, tz), ms per step)."""
+        """Pick the fastest step kernel (the two-kernel step or a tile shape of
+        the fused kernel) on the current state (the state is left unchanged).
+        Returns ((tx, ty, tz), ms per step); (0, 0, 0) is the two-kernel step."""
         t = (ctypes.c_int * 3)()
         ms = ctypes.c_float()
         nat.check(self._lib.lbm_autotune(self._h, int(reps), nat.stream_ptr(stream), t, ctypes.byref(ms)),
@@ -377,8 +378,15 @@ class AllenCahnSolver:
         return (t[0], t[1], t[2]), float(ms.value)
 
     def set_tile(self, tx, ty, tz):
-        """Tile extents of the step kernel (0 = automatic)."""
+        """Step kernel selection: (0, 0, 0) the two-kernel streaming step (the
+        default), else the fused tiled kernel with these tile extents."""
         nat.check(self._lib.lbm_set_tile(self._h, int(tx), int(ty), int(tz)), "lbm_set_tile")
+
+    def get_tile(self):
+        """The current step kernel selection ((0, 0, 0) = two-kernel step)."""
+        t = (ctypes.c_int * 3)()
+        nat.check(self._lib.lbm_get_tile(self._h, t), "lbm_get_tile")
+        return tuple(t)
 
     def status(self):
         v = ctypes.c_uint32()
