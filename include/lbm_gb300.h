@@ -220,6 +220,45 @@ int lbm_measure_static(int64_t nx, int64_t ny, int64_t nz, const void* phi, int 
 /* Sticky status flags (LBM_STATUS_*) accumulated by the device; synchronises. */
 int lbm_status(LbmHandle* h, uint32_t* flags);
 
+/* Bytes of device memory lbm_create allocates for an nx*ny*nz grid of the
+ * given precision (the admission size of a case).  No GPU needed.  No
+ * reference counterpart. */
+int lbm_footprint(int64_t nx, int64_t ny, int64_t nz, int precision, int64_t* bytes);
+
+/*
+ * Batches: many independent grids (handles) that advance together, one launch
+ * of each step kernel per time step for all of them (a block finds its case
+ * in a block -> case table), replayed from a captured two-step CUDA graph.
+ * Each case's arithmetic and reductions are its own, so its results are
+ * bit-identical to stepping it alone.  The handles stay usable on their own
+ * (fields, measure, ...) between batch calls and must outlive the batch.  No
+ * reference counterpart: the reference steps one grid at a time (its sweep
+ * drivers, scripts/run_thesis_sweep.py, loop over cases).
+ */
+typedef struct LbmBatch LbmBatch;
+
+/* Batch of n handles of one precision on the current device, each with its
+ * geometry set.  Allocates the case tables. */
+int lbm_batch_create(LbmHandle* const* handles, int n, LbmBatch** out);
+
+/* Advance every case by nsteps steps on `stream` (asynchronous).  If a case
+ * is in its first step after init, every case takes that one step through the
+ * single-grid kernels first.  Waits for the previous call's table upload. */
+int lbm_batch_step(LbmBatch* b, int nsteps, void* stream);
+
+/* Number of cases. */
+int lbm_batch_size(LbmBatch* b, int* ncases);
+
+/* Autotuner of the batched phi kernel's nodes per thread (its block count per
+ * case): times `reps` batched steps that re-read the current state for each
+ * candidate and keeps the fastest; the state is left unchanged.  Every case
+ * must have taken a step.  Synchronises `stream`; allocates temporary copies
+ * of u.  Outputs (may be NULL): the choice and its time per step in ms. */
+int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread, float* best_ms);
+
+/* Free the batch (not its handles). */
+int lbm_batch_destroy(LbmBatch* b);
+
 /* Message for the last error on the calling thread ("" if none). */
 const char* lbm_last_error(void);
 

@@ -34,6 +34,14 @@ cudaError_t launch_measure(int, int, int, const T*, const uint8_t*, double*, int
                            cudaStream_t);
 template <typename T>
 cudaError_t launch_measure_static(int, int, int, const T*, const uint8_t*, double*, cudaStream_t);
+template <typename T, typename S>
+cudaError_t launch_phi_batch(const void*, const unsigned short*, int, cudaStream_t);
+template <typename T, typename S>
+cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, cudaStream_t);
+template <typename T, typename S>
+size_t case_desc_bytes();
+template <typename T, typename S>
+void fill_case_desc(void*, const Consts<T>&, const State<T, S>&, int, int, int, int);
 }  // namespace lbm
 
 using namespace lbm;
@@ -91,6 +99,12 @@ struct LbmHandle {
   int c_last = 0;         // cbuf slot of the last step's correction
   int64_t steps = 0;
   bool last_raw_in = true;  // mode of the last step's input (for P read-out)
+  // the two-kernel step runs the batched kernels on a one-case table: device
+  // descriptors for the two step parities, valid while desc_ok
+  void* desc = nullptr;
+  bool desc_ok = false;
+  int desc_cur0 = 0;        // cur when the descriptors were filled (parity 0)
+  int phi_per_thread = 16;  // nodes per thread of the phi kernel
 };
 
 namespace {
@@ -267,8 +281,8 @@ Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz, i
 }
 
 void free_all(LbmHandle* h) {
-  void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u, h->phi[0], h->phi[1], h->eps,
-                  h->cls, h->wn, h->partials, h->counters, h->cbuf, h->scal, h->meas_phi};
+  void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u,        h->phi[0], h->phi[1], h->eps,
+                  h->cls,  h->wn,   h->partials, h->counters, h->cbuf, h->scal, h->meas_phi, h->desc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -280,15 +294,73 @@ const Consts<float>& consts_of<float>(const LbmHandle& h) { return h.kf; }
 template <>
 const Consts<double>& consts_of<double>(const LbmHandle& h) { return h.kd; }
 
+bool omega1_of(const LbmHandle* h) {
+  return h->prec == LBM_F64 ? consts_of<double>(*h).omega_f == 1.0 : consts_of<float>(*h).omega_f == 1.0f;
+}
+
+// Blocks of a case in the (batched) phi kernel grid, per_thread nodes per
+// thread, and in the update kernel grid (one node per thread).
+int phi_blocks_of(const LbmHandle* h, int per_thread) {
+  const long long per = (long long)kBlock * per_thread;
+  return (int)std::max<long long>(1, (h->N + per - 1) / per);
+}
+int upd_blocks_of(const LbmHandle* h) { return (int)((h->N + kBlock - 1) / kBlock); }
+
+// The handle's one-case descriptor table for the batched kernels: [0] the
+// state as it is now, [1] after one more step.  The descriptor holds device
+// pointers that alternate with the step parity, constants and grid extents.
+template <typename T, typename S>
+int fill_desc(LbmHandle* h, cudaStream_t st) {
+  const size_t db = case_desc_bytes<T, S>();
+  if (!h->desc) CUDA_TRY(cudaMalloc(&h->desc, 2 * db));
+  std::vector<unsigned char> buf(2 * db);
+  for (int par = 0; par < 2; ++par) {
+    State<T, S> s = make_state<T, S>(*h, h->cur ^ par, h->pc ^ par);
+    s.c_prev = h->c_last ^ par;
+    s.c_cur = h->c_last ^ par ^ 1;
+    fill_case_desc<T, S>(buf.data() + par * db, consts_of<T>(*h), s, 0, phi_blocks_of(h, h->phi_per_thread), 0,
+                         upd_blocks_of(h));
+  }
+  // earlier steps on `st` may still read the old table
+  CUDA_TRY(cudaStreamSynchronize(st));
+  CUDA_TRY(cudaMemcpy(h->desc, buf.data(), 2 * db, cudaMemcpyHostToDevice));
+  h->desc_ok = true;
+  h->desc_cur0 = h->cur;
+  return LBM_OK;
+}
+
+// Launches the step that would run next (no bookkeeping): the first step
+// after init and the fused kernel through launch_step; every other
+// two-kernel step through the batched kernels on the handle's one-case table,
+// so a grid gives the same results alone and in a batch.  `mid` (may be null)
+// is recorded between the two kernels (before the fused kernel).
+template <typename T, typename S>
+int launch_next(LbmHandle* h, const Tiling& t, cudaStream_t st, cudaEvent_t mid) {
+  if (t.tx == 0 && !h->raw && !h->first) {
+    if (!h->desc_ok) {
+      const int rc = fill_desc<T, S>(h, st);
+      if (rc != LBM_OK) return rc;
+    }
+    const int par = (h->cur ^ h->desc_cur0) & 1;
+    const unsigned char* d = static_cast<const unsigned char*>(h->desc) + par * case_desc_bytes<T, S>();
+    CUDA_TRY((launch_phi_batch<T, S>(d, nullptr, phi_blocks_of(h, h->phi_per_thread), st)));
+    if (mid) CUDA_TRY(cudaEventRecord(mid, st));
+    CUDA_TRY((launch_update_batch<T, S>(d, nullptr, upd_blocks_of(h), omega1_of(h), st)));
+    return LBM_OK;
+  }
+  State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
+  s.c_prev = h->c_last;
+  s.c_cur = h->c_last ^ 1;
+  CUDA_TRY(launch_step<T>(consts_of<T>(*h), s, t, h->raw, h->first, st, mid));
+  return LBM_OK;
+}
+
 template <typename T, typename S>
 int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr) {
-  const Consts<T>& k = consts_of<T>(*h);
   for (int i = 0; i < nsteps; ++i) {
-    State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
-    s.c_prev = h->c_last;
-    s.c_cur = h->c_last ^ 1;
     if (ev) CUDA_TRY(cudaEventRecord(ev[2 * i], st));
-    CUDA_TRY(launch_step<T>(k, s, h->tiling, h->raw, h->first, st, ev ? ev[2 * i + 1] : nullptr));
+    const int rc = launch_next<T, S>(h, h->tiling, st, ev ? ev[2 * i + 1] : nullptr);
+    if (rc != LBM_OK) return rc;
     h->last_raw_in = h->raw;
     h->cur ^= 1;
     h->pc ^= 1;
@@ -310,13 +382,11 @@ namespace {
 template <typename T, typename S>
 int time_tiling(LbmHandle* h, const Tiling& t, int reps, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
                 float* ms) {
-  const Consts<T>& k = consts_of<T>(*h);
-  State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
-  s.c_prev = h->c_last;
-  s.c_cur = h->c_last ^ 1;
-  CUDA_TRY(launch_step<T>(k, s, t, h->raw, h->first, st));  // warm-up (sets smem attribute)
+  int rc = launch_next<T, S>(h, t, st, nullptr);  // warm-up (sets smem attributes)
+  if (rc != LBM_OK) return rc;
   CUDA_TRY(cudaEventRecord(e0, st));
-  for (int i = 0; i < reps; ++i) CUDA_TRY(launch_step<T>(k, s, t, h->raw, h->first, st));
+  for (int i = 0; i < reps && rc == LBM_OK; ++i) rc = launch_next<T, S>(h, t, st, nullptr);
+  if (rc != LBM_OK) return rc;
   CUDA_TRY(cudaEventRecord(e1, st));
   CUDA_TRY(cudaEventSynchronize(e1));
   CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
@@ -324,9 +394,52 @@ int time_tiling(LbmHandle* h, const Tiling& t, int reps, cudaStream_t st, cudaEv
 }
 }  // namespace
 
+namespace {
+// Device bytes of one handle's arrays (what lbm_create allocates).
+struct Sizes {
+  size_t pop, u, phi, eps, cls, wn, partials, counters, cbuf, scal, meas_phi;
+  size_t total() const {
+    return 4 * pop + u + 2 * phi + eps + cls + wn + partials + counters + cbuf + scal + meas_phi;
+  }
+};
+Sizes sizes_of(int64_t nx, int64_t ny, int64_t nz, int precision) {
+  const int64_t N = nx * ny * nz;
+  const int64_t Np = (N + kAlignNodes - 1) / kAlignNodes * kAlignNodes;
+  const size_t T = precision == LBM_F64 ? 8 : 4;
+  const size_t P = precision == LBM_F64 ? 8 : (precision == LBM_F16 ? 2 : 4);
+  // per-block partial sums: init (one block per 256 nodes), step (one per
+  // tile; tile extents are at least 2) and measure
+  const int nblocks = (int)((N + kBlock - 1) / kBlock);
+  const size_t max_tiles = (size_t)((nx + 1) / 2) * (size_t)((ny + 1) / 2) * (size_t)((nz + 1) / 2);
+  const size_t npart = std::max<size_t>({(size_t)nblocks, max_tiles, (size_t)kMeasureBlocks * kMeasVals});
+  Sizes z;
+  z.pop = (size_t)Q * Np * P;  // one of f[0], f[1], g[0], g[1]
+  z.u = 3 * Np * T;
+  z.phi = Np * T;  // phi and class arrays padded to Np like the populations
+  z.eps = N * T;
+  z.cls = Np;
+  z.wn = 3 * N * sizeof(float);
+  z.partials = npart * sizeof(double);
+  z.counters = 4 * sizeof(unsigned);
+  z.cbuf = 2 * T;
+  z.scal = 16 * sizeof(double);
+  z.meas_phi = N * T;
+  return z;
+}
+}  // namespace
+
 extern "C" {
 
 const char* lbm_last_error(void) { return g_err.c_str(); }
+
+int lbm_footprint(int64_t nx, int64_t ny, int64_t nz, int precision, int64_t* bytes) {
+  if (!bytes) return fail(LBM_E_ARG, "lbm_footprint: null argument");
+  if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_footprint: 3-D grids with every extent >= 2 only");
+  if (precision != LBM_F32 && precision != LBM_F64 && precision != LBM_F16)
+    return fail(LBM_E_ARG, "lbm_footprint: bad precision");
+  *bytes = (int64_t)sizes_of(nx, ny, nz, precision).total();
+  return LBM_OK;
+}
 
 const char* lbm_version(void) { return "lbm_gb300 0.1 (sm_103a)"; }
 
@@ -357,30 +470,26 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   cudaGetDevice(&h->device);
   const size_t T = h->tsize;
   h->tiling = make_tiling(nx, ny, nz, 0, 0, 0, precision);
-  // per-block partial sums: init (one block per 256 nodes), step (one per
-  // tile; tile extents are at least 2) and measure
-  const int nblocks = (int)((N + kBlock - 1) / kBlock);
-  const size_t max_tiles = (size_t)((nx + 1) / 2) * (size_t)((ny + 1) / 2) * (size_t)((nz + 1) / 2);
-  const size_t npart = std::max<size_t>({(size_t)nblocks, max_tiles, (size_t)kMeasureBlocks * kMeasVals});
+  const Sizes z = sizes_of(nx, ny, nz, precision);
   cudaError_t e = cudaSuccess;
   auto A = [&](void** p, size_t bytes) {
     if (e == cudaSuccess) e = cudaMalloc(p, bytes);
   };
   for (int b = 0; b < 2; ++b) {
-    A(&h->f[b], (size_t)Q * Np * h->psize);
-    A(&h->g[b], (size_t)Q * Np * h->psize);
+    A(&h->f[b], z.pop);
+    A(&h->g[b], z.pop);
   }
-  A(&h->u, 3 * Np * T);
-  A(&h->phi[0], Np * T);  // phi and class arrays padded to Np like the populations
-  A(&h->phi[1], Np * T);
-  A(&h->eps, N * T);
-  A((void**)&h->cls, Np);
-  A((void**)&h->wn, 3 * N * sizeof(float));
-  A((void**)&h->partials, npart * sizeof(double));
-  A((void**)&h->counters, 4 * sizeof(unsigned));
-  A(&h->cbuf, 2 * T);
-  A((void**)&h->scal, 16 * sizeof(double));
-  A(&h->meas_phi, N * T);
+  A(&h->u, z.u);
+  A(&h->phi[0], z.phi);
+  A(&h->phi[1], z.phi);
+  A(&h->eps, z.eps);
+  A((void**)&h->cls, z.cls);
+  A((void**)&h->wn, z.wn);
+  A((void**)&h->partials, z.partials);
+  A((void**)&h->counters, z.counters);
+  A(&h->cbuf, z.cbuf);
+  A((void**)&h->scal, z.scal);
+  A(&h->meas_phi, z.meas_phi);
   if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(h->phi[0], 0, Np * T);
   if (e == cudaSuccess) e = cudaMemset(h->phi[1], 0, Np * T);
@@ -425,6 +534,7 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
   h->kf = make_consts<float>(*h, lut);
   h->kd = make_consts<double>(*h, lut);
   h->geometry_set = true;
+  h->desc_ok = false;
   return LBM_OK;
 }
 
@@ -459,6 +569,7 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
   });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_init_fields: ") + cudaGetErrorString(e));
   h->initialized = true;
+  h->desc_ok = false;
   h->raw = true;
   h->first = true;
   h->c_last = 0;
@@ -549,18 +660,33 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
     }
   }
   Tiling best = h->tiling;
+  int best_per = h->phi_per_thread;
   float best_t = 1e30f;
   int rc = LBM_OK;
   for (const Tiling& t : cands) {
-    float ms = 0.f;
-    rc = with_types(h->prec, [&](auto tag) {
-      return time_tiling<typename decltype(tag)::T, typename decltype(tag)::S>(h, t, reps, st, e0, e1, &ms);
-    });
-    if (rc != LBM_OK) break;
-    if (ms < best_t) {
-      best_t = ms;
-      best = t;
+    // the two-kernel step: also its phi kernel's nodes per thread
+    const std::vector<int> pers = t.tx == 0 ? std::vector<int>{4, 8, 16, 32} : std::vector<int>{h->phi_per_thread};
+    for (int per : pers) {
+      if (per != h->phi_per_thread) {
+        h->phi_per_thread = per;
+        h->desc_ok = false;
+      }
+      float ms = 0.f;
+      rc = with_types(h->prec, [&](auto tag) {
+        return time_tiling<typename decltype(tag)::T, typename decltype(tag)::S>(h, t, reps, st, e0, e1, &ms);
+      });
+      if (rc != LBM_OK) break;
+      if (ms < best_t) {
+        best_t = ms;
+        best = t;
+        best_per = per;
+      }
     }
+    if (rc != LBM_OK) break;
+  }
+  if (h->phi_per_thread != best_per) {
+    h->phi_per_thread = best_per;
+    h->desc_ok = false;
   }
   cudaMemcpyAsync(h->u, u_save, ub, cudaMemcpyDeviceToDevice, st);
   cudaStreamSynchronize(st);
@@ -736,3 +862,295 @@ int lbm_measure_static(int64_t nx, int64_t ny, int64_t nz, const void* phi, int 
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_measure_static: ") + cudaGetErrorString(e));
   return LBM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batches of independent grids (one launch per kernel per step for all)
+// ---------------------------------------------------------------------------
+struct LbmBatch {
+  std::vector<LbmHandle*> h;  // launch order: the cases with omega_f == 1 first
+  int prec = LBM_F32;
+  int device = 0;
+  int n_om1 = 0;            // cases [0, n_om1) have omega_f == 1
+  int phi_per_thread = 16;  // nodes per k_phi_batch thread
+  size_t desc = 0;          // bytes of one case descriptor
+  void* table[2] = {nullptr, nullptr};  // device descriptors: [0] this step, [1] the next
+  unsigned char* staging = nullptr;     // pinned host copy of both tables
+  cudaEvent_t staged = nullptr;         // the last copy out of `staging` has run
+  unsigned short* b2c = nullptr;        // block -> case: k_phi grid, then k_update (omega_f == 1, then other)
+  int phi_blocks = 0, upd_blocks[2] = {0, 0};
+  cudaStream_t cap = nullptr;           // stream used to capture the two-step graph
+  cudaGraphExec_t graph = nullptr;
+};
+
+namespace {
+
+// Block -> case tables (device) for the current phi_per_thread; drops the graph.
+int batch_layout(LbmBatch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  if (b->b2c) cudaFree(b->b2c);
+  b->b2c = nullptr;
+  const int n = (int)b->h.size();
+  long long pb = 0, ub[2] = {0, 0};
+  for (int i = 0; i < n; ++i) {
+    pb += phi_blocks_of(b->h[i], b->phi_per_thread);
+    ub[i < b->n_om1 ? 0 : 1] += upd_blocks_of(b->h[i]);
+  }
+  if (pb > 0x7fffffff || ub[0] + ub[1] > 0x7fffffff) return fail(LBM_E_ARG, "lbm_batch: grids too large");
+  b->phi_blocks = (int)pb;
+  b->upd_blocks[0] = (int)ub[0];
+  b->upd_blocks[1] = (int)ub[1];
+  std::vector<unsigned short> t((size_t)(pb + ub[0] + ub[1]));
+  size_t at[3] = {0, (size_t)pb, (size_t)(pb + ub[0])};
+  for (int i = 0; i < n; ++i) {
+    for (int k = phi_blocks_of(b->h[i], b->phi_per_thread); k > 0; --k) t[at[0]++] = (unsigned short)i;
+    size_t& a = at[i < b->n_om1 ? 1 : 2];
+    for (int k = upd_blocks_of(b->h[i]); k > 0; --k) t[a++] = (unsigned short)i;
+  }
+  CUDA_TRY(cudaMalloc(&b->b2c, t.size() * sizeof(unsigned short)));
+  CUDA_TRY(cudaMemcpy(b->b2c, t.data(), t.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
+  return LBM_OK;
+}
+
+// Descriptors of every case for this step (parity 0) and the next (parity 1).
+template <typename T, typename S>
+void batch_fill_t(LbmBatch* b) {
+  const int n = (int)b->h.size();
+  int pb = 0, ub[2] = {0, 0};
+  for (int i = 0; i < n; ++i) {
+    LbmHandle* h = b->h[i];
+    const int phin = phi_blocks_of(h, b->phi_per_thread), updn = upd_blocks_of(h), g = i < b->n_om1 ? 0 : 1;
+    for (int par = 0; par < 2; ++par) {
+      State<T, S> s = make_state<T, S>(*h, h->cur ^ par, h->pc ^ par);
+      s.c_prev = h->c_last ^ par;
+      s.c_cur = h->c_last ^ par ^ 1;
+      fill_case_desc<T, S>(b->staging + ((size_t)par * n + i) * b->desc, consts_of<T>(*h), s, pb, phin, ub[g],
+                           updn);
+    }
+    pb += phin;
+    ub[g] += updn;
+  }
+}
+
+int batch_fill(LbmBatch* b, cudaStream_t st) {
+  // the previous copy out of the staging buffer must have run before it is rewritten
+  CUDA_TRY(cudaEventSynchronize(b->staged));
+  with_types(b->prec, [&](auto tag) {
+    batch_fill_t<typename decltype(tag)::T, typename decltype(tag)::S>(b);
+    return 0;
+  });
+  const size_t bytes = b->h.size() * b->desc;
+  CUDA_TRY(cudaMemcpyAsync(b->table[0], b->staging, bytes, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(b->table[1], b->staging + bytes, bytes, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaEventRecord(b->staged, st));
+  return LBM_OK;
+}
+
+// One batched step reading descriptor table `par`: k_phi over every case, then
+// k_update over the omega_f == 1 cases and over the others.
+template <typename T, typename S>
+cudaError_t batch_launch_t(LbmBatch* b, int par, cudaStream_t st) {
+  cudaError_t e = launch_phi_batch<T, S>(b->table[par], b->b2c, b->phi_blocks, st);
+  if (e == cudaSuccess)
+    e = launch_update_batch<T, S>(b->table[par], b->b2c + b->phi_blocks, b->upd_blocks[0], true, st);
+  if (e == cudaSuccess)
+    e = launch_update_batch<T, S>(b->table[par], b->b2c + b->phi_blocks + b->upd_blocks[0], b->upd_blocks[1],
+                                  false, st);
+  return e;
+}
+cudaError_t batch_launch(LbmBatch* b, int par, cudaStream_t st) {
+  return with_types(b->prec, [&](auto tag) {
+    return batch_launch_t<typename decltype(tag)::T, typename decltype(tag)::S>(b, par, st);
+  });
+}
+
+// The two-step graph (table 0, then table 1), captured on the batch's own stream.
+int batch_graph(LbmBatch* b) {
+  if (b->graph) return LBM_OK;
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = batch_launch(b, 0, b->cap);
+  if (e == cudaSuccess) e = batch_launch(b, 1, b->cap);
+  const cudaError_t e2 = cudaStreamEndCapture(b->cap, &g);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    b->graph = nullptr;
+    return fail(LBM_E_CUDA, std::string("lbm_batch: graph capture: ") + cudaGetErrorString(e));
+  }
+  return LBM_OK;
+}
+
+void batch_advance(LbmBatch* b, int nsteps) {
+  for (LbmHandle* h : b->h) {
+    if (nsteps & 1) {
+      h->cur ^= 1;
+      h->pc ^= 1;
+      h->c_last ^= 1;
+    }
+    h->steps += nsteps;
+    h->last_raw_in = false;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_batch_create(LbmHandle* const* handles, int n, LbmBatch** out) {
+  if (!handles || !out || n < 1) return fail(LBM_E_ARG, "lbm_batch_create: need at least one handle");
+  *out = nullptr;
+  if (n > 65535) return fail(LBM_E_ARG, "lbm_batch_create: at most 65535 cases");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  for (int i = 0; i < n; ++i) {
+    const LbmHandle* h = handles[i];
+    if (!h || h->prec != handles[0]->prec || h->device != dev || !h->geometry_set)
+      return fail(LBM_E_ARG, "lbm_batch_create: handles must share the precision and the current device and have "
+                             "their geometry set");
+    for (int j = 0; j < i; ++j)
+      if (handles[j] == h) return fail(LBM_E_ARG, "lbm_batch_create: a handle appears twice");
+  }
+  LbmBatch* b = new (std::nothrow) LbmBatch();
+  if (!b) return fail(LBM_E_ARG, "lbm_batch_create: out of host memory");
+  b->prec = handles[0]->prec;
+  b->device = dev;
+  for (int pass = 0; pass < 2; ++pass)
+    for (int i = 0; i < n; ++i)
+      if (omega1_of(handles[i]) == (pass == 0)) b->h.push_back(handles[i]);
+  for (int i = 0; i < n; ++i) b->n_om1 += omega1_of(handles[i]) ? 1 : 0;
+  b->desc = with_types(b->prec, [&](auto tag) {
+    return case_desc_bytes<typename decltype(tag)::T, typename decltype(tag)::S>();
+  });
+  cudaError_t e = cudaMalloc(&b->table[0], n * b->desc);
+  if (e == cudaSuccess) e = cudaMalloc(&b->table[1], n * b->desc);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&b->staging, 2 * n * b->desc);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(b->staged, 0);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    lbm_batch_destroy(b);
+    return fail(LBM_E_CUDA, std::string("lbm_batch_create: ") + cudaGetErrorString(e));
+  }
+  const int rc = batch_layout(b);
+  if (rc != LBM_OK) {
+    lbm_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return LBM_OK;
+}
+
+int lbm_batch_destroy(LbmBatch* b) {
+  if (!b) return LBM_OK;
+  if (b->staged) cudaEventSynchronize(b->staged);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->b2c) cudaFree(b->b2c);
+  if (b->table[0]) cudaFree(b->table[0]);
+  if (b->table[1]) cudaFree(b->table[1]);
+  if (b->staging) cudaFreeHost(b->staging);
+  if (b->staged) cudaEventDestroy(b->staged);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  delete b;
+  return LBM_OK;
+}
+
+int lbm_batch_step(LbmBatch* b, int nsteps, void* stream) {
+  if (!b) return fail(LBM_E_ARG, "lbm_batch_step: null batch");
+  if (nsteps < 0) return fail(LBM_E_ARG, "lbm_batch_step: nsteps must be >= 0");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  bool any_first = false;
+  for (LbmHandle* h : b->h) {
+    if (!h->initialized) return fail(LBM_E_STATE, "lbm_batch_step: a case is not initialised");
+    any_first |= h->raw || h->first;
+  }
+  int rest = nsteps;
+  if (any_first && rest > 0) {
+    // a case in its first step after init reads its populations in place:
+    // every case takes this step through the single-grid kernels (the same
+    // arithmetic), the rest run batched
+    for (LbmHandle* h : b->h) {
+      const int rc = lbm_step(h, 1, stream);
+      if (rc != LBM_OK) return rc;
+    }
+    --rest;
+  }
+  if (rest == 0) return LBM_OK;
+  int rc = batch_fill(b, st);
+  if (rc != LBM_OK) return rc;
+  if (rest >= 2) {
+    rc = batch_graph(b);
+    if (rc != LBM_OK) return rc;
+    for (int i = 0; i < rest / 2; ++i) CUDA_TRY(cudaGraphLaunch(b->graph, st));
+  }
+  // after an even number of steps every case is back at the parity of table 0
+  if (rest & 1) CUDA_TRY(batch_launch(b, 0, st));
+  batch_advance(b, rest);
+  return LBM_OK;
+}
+
+int lbm_batch_size(LbmBatch* b, int* ncases) {
+  if (!b || !ncases) return fail(LBM_E_ARG, "lbm_batch_size: null argument");
+  *ncases = (int)b->h.size();
+  return LBM_OK;
+}
+
+int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread, float* best_ms) {
+  if (!b) return fail(LBM_E_ARG, "lbm_batch_autotune: null batch");
+  if (reps <= 0) reps = 5;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (LbmHandle* h : b->h)
+    if (!h->initialized || h->raw || h->first)
+      return fail(LBM_E_STATE, "lbm_batch_autotune: every case must have taken a step");
+  // time batched steps that re-read the current state (u, updated in place, is restored after)
+  std::vector<void*> usave(b->h.size(), nullptr);
+  for (size_t i = 0; i < b->h.size(); ++i) {
+    const size_t ub = 3 * (size_t)b->h[i]->Np * b->h[i]->tsize;
+    CUDA_TRY(cudaMalloc(&usave[i], ub));
+    CUDA_TRY(cudaMemcpyAsync(usave[i], b->h[i]->u, ub, cudaMemcpyDeviceToDevice, st));
+  }
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  int best = b->phi_per_thread, rc = LBM_OK;
+  float best_t = 1e30f;
+  for (int per : {1, 2, 4, 8, 16, 32}) {
+    b->phi_per_thread = per;
+    rc = batch_layout(b);
+    if (rc == LBM_OK) rc = batch_fill(b, st);
+    if (rc != LBM_OK) break;
+    cudaError_t e = batch_launch(b, 0, st);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = batch_launch(b, 0, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) {
+      rc = fail(LBM_E_CUDA, std::string("lbm_batch_autotune: ") + cudaGetErrorString(e));
+      break;
+    }
+    if (ms < best_t) {
+      best_t = ms;
+      best = per;
+    }
+  }
+  for (size_t i = 0; i < b->h.size(); ++i) {
+    const size_t ub = 3 * (size_t)b->h[i]->Np * b->h[i]->tsize;
+    cudaMemcpyAsync(b->h[i]->u, usave[i], ub, cudaMemcpyDeviceToDevice, st);
+  }
+  cudaStreamSynchronize(st);
+  for (void* p : usave) cudaFree(p);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != LBM_OK) return rc;
+  b->phi_per_thread = best;
+  rc = batch_layout(b);
+  if (rc != LBM_OK) return rc;
+  if (best_per_thread) *best_per_thread = best;
+  if (best_ms) *best_ms = best_t / reps;
+  return LBM_OK;
+}
+
+}  // extern "C"

@@ -27,6 +27,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <mutex>
 #include <type_traits>
 
@@ -141,6 +142,9 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float rcp(float a) { return 1.0f / a; }
+// Fused multiply-add, written out where the step relies on it.
+template <typename T>
+__device__ __forceinline__ T fma_(T a, T b, T c) { return fma(a, b, c); }
 __device__ __forceinline__ double rcp(double a) { return 1.0 / a; }
 
 // q = floor(t / d) for 0 <= t < 2^22 via a float reciprocal: the relative
@@ -168,19 +172,23 @@ __device__ __forceinline__ double block_sum(double v) {
 // partials in block order (deterministic) and returns true in thread 0 with
 // the total in *total.  Resets the counter for the next launch.
 __device__ __forceinline__ bool last_block_total(double part, double* partials, unsigned* counter,
-                                                 double* total) {
+                                                 double* total, int blk = -1, int nblk = -1) {
   __shared__ bool s_last;
+  if (blk < 0) {
+    blk = blockIdx.x;
+    nblk = gridDim.x;
+  }
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = part;
+    partials[blk] = part;
     __threadfence();
     const unsigned done = atomicAdd(counter, 1u);
-    s_last = (done == gridDim.x - 1);
+    s_last = (done == (unsigned)nblk - 1);
   }
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
   double acc = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc += ((volatile double*)partials)[i];
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) acc += ((volatile double*)partials)[i];
   acc = block_sum(acc);
   if (threadIdx.x == 0) {
     *total = acc;
@@ -335,7 +343,7 @@ __device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n,
       if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
     }
     if (FUSED) {
-      lap = lap + k.w2c[q] * (ps[q] - phi);
+      lap = fma_(k.w2c[q], ps[q] - phi, lap);
     } else {
       lap = lap + (T(2) * k.w[q]) * (ps[q] - phi) / k.cs2;
     }
@@ -345,7 +353,7 @@ __device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n,
 // Chemical potential (lbm/fe_ac_solver.py:326-340).
 template <typename T>
 __device__ __forceinline__ T chem_pot(const Consts<T>& k, uint8_t c, T phi, T lap) {
-  T mu = k.beta4 * phi * (phi - T(1)) * (phi - T(0.5)) - k.kappa * lap;
+  T mu = fma_(-k.kappa, lap, k.beta4 * phi * (phi - T(1)) * (phi - T(0.5)));
   if (k.wetting && (c & kBoundary)) {
     if (k.linear) mu = mu + k.mu_wall_add;
     else mu = mu + k.phi_c * phi * (T(1) - phi);
@@ -373,9 +381,6 @@ __device__ __forceinline__ T edot(int q, T a0, T a1, T a2) {
 __host__ __device__ constexpr int pair_first(int i) {
   return i == 0 ? 1 : i == 1 ? 3 : i == 2 ? 5 : i == 3 ? 7 : i == 4 ? 8 : i == 5 ? 11 : i == 6 ? 12 : i == 7 ? 15 : 16;
 }
-
-template <typename T>
-__device__ __forceinline__ T fma_(T a, T b, T c) { return fma(a, b, c); }
 
 // OMEGA1: tau_f == 1 (the reference's default tau_h = 1.0), where the
 // phase-field BGK collision f - (f - f_eq) + src is f_eq + src and the
@@ -456,7 +461,7 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   T gx, gy, gz, lap;
   grad_lap<T, true, State<T, S>, SolidAt, true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
 
-  const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
+  const T rho = fma_(phi, k.rho_l, (T(1) - phi) * k.rho_g);
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
   const T mu = chem_pot(k, c, phi, lap);
 
@@ -503,61 +508,61 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   T sxx, syy, szz, sxy, sxz, syz;
   {
     const T pc = P * k.cs2;
-    sxx = ((sp[0] + (sp[3] + sp[4]) + (sp[5] + sp[6])) - pc) - uo0 * uo0;
-    syy = ((sp[1] + (sp[3] + sp[4]) + (sp[7] + sp[8])) - pc) - uo1 * uo1;
-    szz = ((sp[2] + (sp[5] + sp[6]) + (sp[7] + sp[8])) - pc) - uo2 * uo2;
-    sxy = (sp[3] - sp[4]) - uo0 * uo1;
-    sxz = (sp[5] - sp[6]) - uo0 * uo2;
-    syz = (sp[7] - sp[8]) - uo1 * uo2;
+    sxx = fma_(-uo0, uo0, (sp[0] + (sp[3] + sp[4]) + (sp[5] + sp[6])) - pc);
+    syy = fma_(-uo1, uo1, (sp[1] + (sp[3] + sp[4]) + (sp[7] + sp[8])) - pc);
+    szz = fma_(-uo2, uo2, (sp[2] + (sp[5] + sp[6]) + (sp[7] + sp[8])) - pc);
+    sxy = fma_(-uo0, uo1, sp[3] - sp[4]);
+    sxz = fma_(-uo0, uo2, sp[5] - sp[6]);
+    syz = fma_(-uo1, uo2, sp[7] - sp[8]);
   }
 
   // 5. forces (Fakhari 2017, :416-439)
   T F0 = mu * gx, F1 = mu * gy, F2 = mu * gz;
   if (k.stab_mode <= 1) {
     const T fp = ((-P) * k.drho) * k.cs2;
-    F0 = F0 + fp * gx;
-    F1 = F1 + fp * gy;
-    F2 = F2 + fp * gz;
+    F0 = fma_(fp, gx, F0);
+    F1 = fma_(fp, gy, F1);
+    F2 = fma_(fp, gz, F2);
   }
   if (k.stab_mode == 0) {
-    F0 = F0 + (k.visc * ((sxx * gx + sxy * gy) + sxz * gz)) * k.drho;
-    F1 = F1 + (k.visc * ((sxy * gx + syy * gy) + syz * gz)) * k.drho;
-    F2 = F2 + (k.visc * ((sxz * gx + syz * gy) + szz * gz)) * k.drho;
+    F0 = fma_(k.visc * fma_(sxz, gz, fma_(sxy, gy, sxx * gx)), k.drho, F0);
+    F1 = fma_(k.visc * fma_(syz, gz, fma_(syy, gy, sxy * gx)), k.drho, F1);
+    F2 = fma_(k.visc * fma_(szz, gz, fma_(syz, gy, sxz * gx)), k.drho, F2);
   }
   if (k.has_gforce) {
-    F0 = F0 + k.gforce[0] * rho;
-    F1 = F1 + k.gforce[1] * rho;
-    F2 = F2 + k.gforce[2] * rho;
+    F0 = fma_(k.gforce[0], rho, F0);
+    F1 = fma_(k.gforce[1], rho, F1);
+    F2 = fma_(k.gforce[2], rho, F2);
   }
 
   // 6. velocity (:442-447)
   T u0, u1, u2;
   {
     const T hr = T(0.5) * rcp(rho_eff);
-    u0 = (dp[0] + (dp[3] - dp[4]) + (dp[5] - dp[6])) + F0 * hr;
-    u1 = (dp[1] + (dp[3] + dp[4]) + (dp[7] - dp[8])) + F1 * hr;
-    u2 = (dp[2] + (dp[5] + dp[6]) + (dp[7] + dp[8])) + F2 * hr;
+    u0 = fma_(F0, hr, dp[0] + (dp[3] - dp[4]) + (dp[5] - dp[6]));
+    u1 = fma_(F1, hr, dp[1] + (dp[3] + dp[4]) + (dp[7] - dp[8]));
+    u2 = fma_(F2, hr, dp[2] + (dp[5] + dp[6]) + (dp[7] + dp[8]));
     if (c & kSolid) u0 = u1 = u2 = T(0);
   }
-  const T b = ((u0 * u0 + u1 * u1) + u2 * u2) * k.inv_two_cs2;
+  const T b = fma_(u2, u2, fma_(u1, u1, u0 * u0)) * k.inv_two_cs2;
 
   // 7. Allen-Cahn source (:450-494)
   T S0, S1, S2;
   {
     T d0 = T(0), d1 = T(0), d2 = T(0);
     if (!FIRST) {
-      d0 = phi * u0 - pp * uo0;
-      d1 = phi * u1 - pp * uo1;
-      d2 = phi * u2 - pp * uo2;
+      d0 = fma_(phi, u0, -pp * uo0);
+      d1 = fma_(phi, u1, -pp * uo1);
+      d2 = fma_(phi, u2, -pp * uo2);
     }
-    T gm = sqrt((gx * gx + gy * gy) + gz * gz);
+    T gm = sqrt(fma_(gz, gz, fma_(gy, gy, gx * gx)));
     gm = gm < T(1e-10) ? T(1e-10) : gm;
     const T lam = ((T(4) * phi) * (T(1) - phi)) * k.inv_W;
     T cl = k.cs2 * lam * k.ac_scale * rcp(gm);
     if (k.wetting) cl = cl * (T(1) - k.sharpen_reduce * k.ww[c >> kWwShift]);
-    S0 = d0 + cl * gx;
-    S1 = d1 + cl * gy;
-    S2 = d2 + cl * gz;
+    S0 = fma_(cl, gx, d0);
+    S1 = fma_(cl, gy, d1);
+    S2 = fma_(cl, gz, d2);
   }
 
   // 8. both BGK collisions (:496-530) one opposite pair (q, opp q) at a time.
@@ -658,12 +663,18 @@ struct TileSum<float> {
 
 // Block total of the tile sums, published; the last block to finish adds the
 // block totals in block order and returns true in thread 0 with the grid
-// total in *total (NaN if any phi was NaN).  Resets the counter.
+// total in *total (NaN if any phi was NaN).  Resets the counter.  blk / nblk:
+// this block's index among the blocks that share the sum and their number
+// (default: the launch grid).
 template <typename T>
 __device__ __forceinline__ bool grid_phi_total(TileSum<T>& ts, double* partials, unsigned* counter,
-                                               double* total) {
+                                               double* total, int blk = -1, int nblk = -1) {
+  if (blk < 0) {
+    blk = blockIdx.x;
+    nblk = gridDim.x;
+  }
   if constexpr (sizeof(T) == 8) {
-    return last_block_total(block_sum(ts.a), partials, counter, total);
+    return last_block_total(block_sum(ts.a), partials, counter, total, blk, nblk);
   } else {
     __shared__ unsigned long long s_warp[kBlock / 32];
     __shared__ bool s_last;
@@ -679,16 +690,16 @@ __device__ __forceinline__ bool grid_phi_total(TileSum<T>& ts, double* partials,
       unsigned long long r = 0ull;
 #pragma unroll
       for (int i = 0; i < kBlock / 32; ++i) r += s_warp[i];
-      up[blockIdx.x] = nan ? kSumNaN : r;
+      up[blk] = nan ? kSumNaN : r;
       __threadfence();
-      s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+      s_last = (atomicAdd(counter, 1u) == (unsigned)nblk - 1);
     }
     __syncthreads();
     if (!s_last) return false;
     __threadfence();
     unsigned long long acc = 0ull;
     bool any_nan = false;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
       const unsigned long long p = ((volatile unsigned long long*)up)[i];
       if (p == kSumNaN) any_nan = true;
       else acc += p;
@@ -896,29 +907,32 @@ __device__ __forceinline__ void decode(const FastDiv& dz, const FastDiv& dy, int
 
 // Persistent: a grid of about one wave strides over the nodes, so that the
 // per-block publication of the partial sum happens once per block.
+// phi of node n (written to phi_out) added to the block's sum.
 template <typename T, typename S, bool RAW>
-__global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
-  const Pol pol = Pol::make();
-  TileSum<T> part;
-  for (int n = blockIdx.x * kBlock + threadIdx.x; n < k.N; n += gridDim.x * kBlock) {
-    const uint8_t c = s.cls[n];
-    T phi = T(0);
-    if (!(c & kSolid)) {
-      int ix, iy, iz;
-      decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
-      const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
-      const T eps = (c & kPartial) ? s.eps[n] : T(0);
-      T v[Q];
-      // f is read again by k_update only when omega_f != 1
-      fetch_f<T, S, RAW, true>(v, k, s, n, (size_t)k.N, nb, c, eps, k.omega_f == T(1) ? pol.once : pol.keep);
-      phi = clamp01(seqsum(v));
-    }
-    st_pol(s.phi_out + n, phi, pol.keep);  // read back (stencil) by k_update
-    part.add(phi);
+__device__ __forceinline__ void phi_node(const Consts<T>& k, const State<T, S>& s, int n, const Pol& pol,
+                                         TileSum<T>& part) {
+  const uint8_t c = s.cls[n];
+  T phi = T(0);
+  if (!(c & kSolid)) {
+    int ix, iy, iz;
+    decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
+    const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
+    const T eps = (c & kPartial) ? s.eps[n] : T(0);
+    T v[Q];
+    // f is read again by k_update only when omega_f != 1
+    fetch_f<T, S, RAW, true>(v, k, s, n, (size_t)k.N, nb, c, eps, k.omega_f == T(1) ? pol.once : pol.keep);
+    phi = clamp01(seqsum(v));
   }
-  // sum(phi) of the grid -> mass-correction factor of this step (:582-589)
+  st_pol(s.phi_out + n, phi, pol.keep);  // read back (stencil) by k_update
+  part.add(phi);
+}
+
+// sum(phi) of the grid -> mass-correction factor of this step (:582-589),
+// computed by the last of the grid's nblk blocks to finish.
+template <typename T, typename S>
+__device__ __forceinline__ void phi_finish(const State<T, S>& s, TileSum<T>& part, int blk, int nblk) {
   double total;
-  if (grid_phi_total<T>(part, s.partials, s.counter, &total)) {
+  if (grid_phi_total<T>(part, s.partials, s.counter, &total, blk, nblk)) {
     const T sum = (T)total;
     T corr = T(1);
     if (sum > T(1e-6)) {
@@ -931,6 +945,14 @@ __global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
     s.cbuf[s.c_cur] = corr;
     s.scal[1] = total;
   }
+}
+
+template <typename T, typename S, bool RAW>
+__global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
+  const Pol pol = Pol::make();
+  TileSum<T> part;
+  for (int n = blockIdx.x * kBlock + threadIdx.x; n < k.N; n += gridDim.x * kBlock) phi_node<T, S, RAW>(k, s, n, pol, part);
+  phi_finish(s, part, blockIdx.x, gridDim.x);
 }
 
 template <typename T, typename S>
@@ -960,6 +982,54 @@ template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
 __global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_update(Consts<T> k, State<T, S> s) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
   if (n < k.N) update_one<T, S, RAW, FIRST, OMEGA1>(k, s, n, Pol::make());
+}
+
+// ---------------------------------------------------------------------------
+// Batched step: many independent grids advance in one launch of each kernel
+// (a single grid uses the same kernels with a one-case table and no block ->
+// case table, so that it gives the same results alone and in a batch).
+// A block finds its case in a block -> case table and copies the case's
+// constants and state pointers (CaseDesc) into shared memory; the arithmetic
+// per node is the single-grid step's, and each case's sum of phi is reduced
+// over that case's blocks only, so a case gives bit-identical results alone
+// and in a batch.  Cases in their first step after init are not batched.
+// ---------------------------------------------------------------------------
+template <typename T, typename S>
+struct CaseDesc {
+  Consts<T> k;
+  State<T, S> s;
+  int phi_blk0, phi_nblk;  // the case's blocks in the k_phi_batch grid
+  int upd_blk0, upd_nblk;  // and in the k_update_batch grid
+};
+
+template <typename D>
+__device__ __forceinline__ void load_desc(D& dst, const D* src) {
+  static_assert(sizeof(D) % 4 == 0, "descriptor copied as 32-bit words");
+  const unsigned* a = reinterpret_cast<const unsigned*>(src);
+  unsigned* b = reinterpret_cast<unsigned*>(&dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(D) / 4); i += blockDim.x) b[i] = __ldg(a + i);
+  __syncthreads();
+}
+
+template <typename T, typename S>
+__global__ void __launch_bounds__(kBlock) k_phi_batch(const CaseDesc<T, S>* __restrict__ cases,
+                                                     const unsigned short* __restrict__ blk2case) {
+  __shared__ CaseDesc<T, S> d;
+  load_desc(d, cases + (blk2case ? blk2case[blockIdx.x] : 0));
+  const Pol pol = Pol::make();
+  const int b = blockIdx.x - d.phi_blk0, nb = d.phi_nblk;
+  TileSum<T> part;
+  for (int n = b * kBlock + threadIdx.x; n < d.k.N; n += nb * kBlock) phi_node<T, S, false>(d.k, d.s, n, pol, part);
+  phi_finish(d.s, part, b, nb);
+}
+
+template <typename T, typename S, bool OMEGA1>
+__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_update_batch(
+    const CaseDesc<T, S>* __restrict__ cases, const unsigned short* __restrict__ blk2case) {
+  __shared__ CaseDesc<T, S> d;
+  load_desc(d, cases + (blk2case ? blk2case[blockIdx.x] : 0));
+  const int n = (blockIdx.x - d.upd_blk0) * kBlock + threadIdx.x;
+  if (n < d.k.N) update_one<T, S, false, false, OMEGA1>(d.k, d.s, n, Pol::make());
 }
 
 // Grid of a persistent kernel: resident blocks per SM x SMs (one wave), at
@@ -1270,6 +1340,43 @@ cudaError_t launch_step(const Consts<T>& k, const State<T, S>& s, const Tiling& 
              : launch_step_t<T, S, false, false, false>(k, s, tl, st);
 }
 
+// Batched step kernels over a device case table; phi_blocks / upd_blocks:
+// total blocks of the two grids (the lengths of the block -> case tables).
+template <typename T, typename S>
+cudaError_t launch_phi_batch(const void* cases, const unsigned short* b2c, int blocks, cudaStream_t st) {
+  if (blocks <= 0) return cudaSuccess;
+  k_phi_batch<T, S><<<blocks, kBlock, 0, st>>>(static_cast<const CaseDesc<T, S>*>(cases), b2c);
+  return cudaGetLastError();
+}
+template <typename T, typename S>
+cudaError_t launch_update_batch(const void* cases, const unsigned short* b2c, int blocks, bool omega1,
+                                cudaStream_t st) {
+  if (blocks <= 0) return cudaSuccess;
+  if (omega1)
+    k_update_batch<T, S, true><<<blocks, kBlock, 0, st>>>(static_cast<const CaseDesc<T, S>*>(cases), b2c);
+  else
+    k_update_batch<T, S, false><<<blocks, kBlock, 0, st>>>(static_cast<const CaseDesc<T, S>*>(cases), b2c);
+  return cudaGetLastError();
+}
+template <typename T, typename S>
+size_t case_desc_bytes() {
+  return sizeof(CaseDesc<T, S>);
+}
+// Fills one descriptor in host memory.
+template <typename T, typename S>
+void fill_case_desc(void* dst, const Consts<T>& k, const State<T, S>& s, int phi_blk0, int phi_nblk, int upd_blk0,
+                    int upd_nblk) {
+  CaseDesc<T, S> d;
+  std::memset(&d, 0, sizeof(d));
+  d.k = k;
+  d.s = s;
+  d.phi_blk0 = phi_blk0;
+  d.phi_nblk = phi_nblk;
+  d.upd_blk0 = upd_blk0;
+  d.upd_nblk = upd_nblk;
+  std::memcpy(dst, &d, sizeof(d));
+}
+
 template <typename T, typename S, typename Src>
 cudaError_t launch_init(const Consts<T>& k, const State<T, S>& s, const Src* phi0, const Src* u0, cudaStream_t st) {
   const int grid = (k.N + kBlock - 1) / kBlock;
@@ -1389,6 +1496,16 @@ LBM_INSTANTIATE(float, float)
 LBM_INSTANTIATE(double, double)
 LBM_INSTANTIATE(float, __half)
 #undef LBM_INSTANTIATE
+
+#define LBM_INSTANTIATE_BATCH(T, S)                                                                             \
+  template cudaError_t launch_phi_batch<T, S>(const void*, const unsigned short*, int, cudaStream_t);           \
+  template cudaError_t launch_update_batch<T, S>(const void*, const unsigned short*, int, bool, cudaStream_t);  \
+  template size_t case_desc_bytes<T, S>();                                                                      \
+  template void fill_case_desc<T, S>(void*, const Consts<T>&, const State<T, S>&, int, int, int, int);
+LBM_INSTANTIATE_BATCH(float, float)
+LBM_INSTANTIATE_BATCH(double, double)
+LBM_INSTANTIATE_BATCH(float, __half)
+#undef LBM_INSTANTIATE_BATCH
 
 template cudaError_t launch_measure<float>(int, int, int, const float*, const uint8_t*, double*, int, unsigned*, double*, cudaStream_t);
 template cudaError_t launch_measure<double>(int, int, int, const double*, const uint8_t*, double*, int, unsigned*, double*, cudaStream_t);

@@ -23,7 +23,8 @@ EXPORTS = (
     "lbm_create", "lbm_destroy", "lbm_set_geometry", "lbm_init_fields", "lbm_step", "lbm_step_profiled",
     "lbm_get_fields", "lbm_get_populations", "lbm_get_geometry", "lbm_geometry_host",
     "lbm_get_scalars", "lbm_measure", "lbm_status", "lbm_last_error", "lbm_version",
-    "lbm_set_tile", "lbm_get_tile", "lbm_autotune", "lbm_measure_static",
+    "lbm_set_tile", "lbm_get_tile", "lbm_autotune", "lbm_measure_static", "lbm_footprint",
+    "lbm_batch_create", "lbm_batch_step", "lbm_batch_size", "lbm_batch_autotune", "lbm_batch_destroy",
 )
 
 
@@ -63,6 +64,12 @@ def _declare(L):
                              ctypes.POINTER(_i64)], _i32),
         "lbm_measure": ([_vp, ctypes.POINTER(_dbl), _vp], _i32),
         "lbm_measure_static": ([_i64, _i64, _i64, _vp, _i32, _vp, _vp, _vp], _i32),
+        "lbm_footprint": ([_i64, _i64, _i64, _i32, ctypes.POINTER(_i64)], _i32),
+        "lbm_batch_create": ([ctypes.POINTER(_vp), _i32, ctypes.POINTER(_vp)], _i32),
+        "lbm_batch_step": ([_vp, _i32, _vp], _i32),
+        "lbm_batch_size": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),
+        "lbm_batch_autotune": ([_vp, _i32, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)], _i32),
+        "lbm_batch_destroy": ([_vp], _i32),
         "lbm_status": ([_vp, ctypes.POINTER(_u32)], _i32),
         "lbm_set_tile": ([_vp, _i32, _i32, _i32], _i32),
         "lbm_get_tile": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),

@@ -164,13 +164,18 @@ class AllenCahnSolver:
         self._cache = {}
 
     def __del__(self):
+        self.close()
+
+    def close(self):
+        """Free the device state now (the solver is unusable afterwards)."""
         h = getattr(self, "_h", None)
         if h is not None and h.value:
             try:
                 self._lib.lbm_destroy(h)
             except Exception:
                 pass
-            self._h = None
+        self._h = None
+        self._cache = {}
 
     # -- setup ----------------------------------------------------------------
     def set_solid(self, solid_mask, solid_fraction=None):

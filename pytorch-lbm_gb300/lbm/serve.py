@@ -1,0 +1,174 @@
+"""Serving loop for droplet-impact requests: continuous batching on one GPU.
+
+Requests (an ``ImpactCase`` and an arrival time) are admitted in arrival
+order as soon as they have arrived and their device footprint fits in the
+HBM budget next to the cases already resident.  Resident cases advance
+together in ticks of batched steps (``AllenCahnBatch``: one launch of each
+step kernel per step for all of them).  A tick is never longer than the
+fewest steps any resident case still needs, so a case stops exactly at its
+step count.  Finished cases are measured and freed at the end of a tick, and
+requests that arrived in the meantime are admitted before the next tick.  A
+case's results do not depend on what it shares the GPU with: the batch
+keeps every case's arithmetic and reductions separate.
+
+Reported per request: arrival, admission and completion times (seconds from
+the start of ``serve``) and the spread diagnostics of the final phi; overall:
+p50 / p99 time to completion and aggregate MLUPS (node updates of all
+requests / wall time).  ``serve_sequential`` runs the same request stream
+through the plain one-case-at-a-time path for comparison.
+
+The scheduling logic talks to the GPU through a backend (``GpuBackend``);
+tests substitute a simulated one.  The reference has no serving loop.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Request:
+    rid: int
+    case: object          # ImpactCase (grid, steps, ...)
+    arrival: float        # seconds after the start of serving
+
+
+@dataclass
+class Result:
+    rid: int
+    arrival: float
+    admitted: float
+    finished: float
+    steps: int
+    nodes: int
+    measure: dict = field(default_factory=dict)
+    phi: object = None    # final phi on the host, if kept
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+def poisson_arrivals(n, rate, seed):
+    """Arrival times of n requests of a Poisson process with `rate` per second."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n)).tolist()
+
+
+class GpuBackend:
+    """Cases as AllenCahnSolver objects on the current CUDA device."""
+
+    def __init__(self, dtype, device="cuda", keep_phi=False):
+        import torch
+        self.torch = torch
+        self.dtype = dtype
+        self.device = device
+        self.keep_phi = keep_phi
+
+    def footprint(self, case):
+        from .batch import footprint
+        return footprint(case.grid, self.dtype)
+
+    def build(self, case):
+        from .impact import build_impact_case
+        return build_impact_case(case, self.dtype, self.device)
+
+    def batch(self, solvers):
+        from .batch import AllenCahnBatch
+        return AllenCahnBatch(solvers)
+
+    def run_alone(self, solver, nsteps):
+        solver.run(nsteps)
+
+    def finish(self, solver):
+        m = solver.measure()
+        phi = solver.phi.cpu().numpy() if self.keep_phi else None
+        solver.close()
+        return m, phi
+
+    def sync(self):
+        self.torch.cuda.synchronize()
+
+
+def _stats(results, wall):
+    lat = np.array([r.latency for r in results]) if results else np.zeros(1)
+    updates = float(sum(r.nodes * r.steps for r in results))
+    return {"requests": len(results), "wall_s": wall, "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+            "mlups": updates / wall / 1e6 if wall > 0 else 0.0}
+
+
+def serve(requests, backend, budget_bytes, tick=100, max_slots=None, clock=time.perf_counter, sleep=time.sleep):
+    """Continuous batching of `requests` under an HBM budget and at most
+    `max_slots` resident cases (None: no limit).  Returns (results in
+    completion order, stats)."""
+    pending = sorted(requests, key=lambda r: r.arrival)
+    for r in pending:
+        if backend.footprint(r.case) > budget_bytes:
+            raise ValueError(f"request {r.rid} needs more than the whole budget")
+    active = {}        # rid -> [request, solver, remaining steps, bytes, admitted]
+    used = 0
+    batch = None
+    members = ()
+    results = []
+    t0 = clock()
+    while pending or active:
+        now = clock() - t0
+        # admit, in arrival order, what has arrived and fits
+        while (pending and pending[0].arrival <= now and used + backend.footprint(pending[0].case) <= budget_bytes
+               and (max_slots is None or len(active) < max_slots)):
+            r = pending.pop(0)
+            b = backend.footprint(r.case)
+            active[r.rid] = [r, backend.build(r.case), int(r.case.steps), b, clock() - t0]
+            used += b
+        if not active:
+            # idle until the next arrival
+            sleep(max(0.0, pending[0].arrival - (clock() - t0)))
+            continue
+        key = tuple(sorted(active))
+        if key != members:
+            if batch is not None:
+                batch.close()
+            batch = backend.batch([active[k][1] for k in key])
+            members = key
+        n = min(tick, min(a[2] for a in active.values()))
+        batch.run(n)
+        done = []
+        for k, a in active.items():
+            a[2] -= n
+            if a[2] == 0:
+                done.append(k)
+        if done:
+            # retire: measuring waits for the batch's steps to finish
+            batch.close()
+            batch, members = None, ()
+            for k in done:
+                r, solver, _, b, adm = active.pop(k)
+                m, phi = backend.finish(solver)
+                results.append(Result(r.rid, r.arrival, adm, clock() - t0, int(r.case.steps), r.case.nodes, m, phi))
+                used -= b
+    if batch is not None:
+        batch.close()
+    backend.sync()
+    return results, _stats(results, clock() - t0)
+
+
+def serve_sequential(requests, backend, clock=time.perf_counter, sleep=time.sleep):
+    """The same request stream through the plain path: one case at a time,
+    in arrival order, each run to completion before the next is built."""
+    pending = sorted(requests, key=lambda r: r.arrival)
+    results = []
+    t0 = clock()
+    for r in pending:
+        wait = r.arrival - (clock() - t0)
+        if wait > 0:
+            sleep(wait)
+        adm = clock() - t0
+        solver = backend.build(r.case)
+        backend.run_alone(solver, int(r.case.steps))
+        m, phi = backend.finish(solver)
+        results.append(Result(r.rid, r.arrival, adm, clock() - t0, int(r.case.steps), r.case.nodes, m, phi))
+    backend.sync()
+    return results, _stats(results, clock() - t0)

@@ -1,0 +1,89 @@
+"""Batched stepping (lbm_batch_*, AllenCahnBatch) against stepping each case
+alone: bit-identical phi, u and populations, for float32 (mixing tau_f = 1
+cases with a tau_h = 0.57 case, i.e. both update kernels in one batch) and
+for the half-precision deviation storage; the batch autotuner leaves the
+state unchanged."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from lbm.impact import ImpactCase, impact_config, impact_inputs  # noqa: E402
+
+CASES = [
+    ImpactCase(0, (24, 24, 20), "flat", 5.0, 120.0, -0.03, 0),
+    ImpactCase(1, (32, 28, 24), "ridge", 6.0, 150.0, -0.05, 0),
+    ImpactCase(2, (28, 28, 28), "convex", 5.5, 100.0, -0.04, 0),
+    ImpactCase(3, (30, 26, 22), "concave", 5.0, 162.0, -0.06, 0),
+]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    return built_lib
+
+
+def _solver(case, dtype, tau_h=None):
+    from lbm.fe_ac_solver import AllenCahnSolver
+    cfg = impact_config(case, "cuda")
+    if tau_h is not None:
+        cfg.tau_h = tau_h
+    solid, frac, C, u = impact_inputs(case)
+    s = AllenCahnSolver(cfg, dtype=dtype, geo_amplification=1.5, geometric_wetting=True)
+    s.set_solid(solid, frac)
+    s.init_fields(C, u)
+    return s
+
+
+def _state(s):
+    phi, u = s.fields("phi", "u")
+    return phi.clone(), u.clone(), s.f.clone(), s.g.clone()
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
+@pytest.mark.parametrize("steps", [[7], [1, 4, 3]])
+def test_batch_matches_cases_alone(dtype, steps):
+    from lbm.batch import AllenCahnBatch
+    taus = [None, 0.57, None, None]
+    alone = [_solver(c, dtype, t) for c, t in zip(CASES, taus)]
+    for s in alone:
+        s.run(sum(steps))
+    mixed = [_solver(c, dtype, t) for c, t in zip(CASES, taus)]
+    b = AllenCahnBatch(mixed)
+    for n in steps:
+        b.run(n)
+    torch.cuda.synchronize()
+    for a, m in zip(alone, mixed):
+        for x, y in zip(_state(a), _state(m)):
+            assert torch.equal(x, y)
+        assert a.scalars() == m.scalars()
+    b.close()
+
+
+def test_batch_autotune_leaves_state_unchanged():
+    from lbm.batch import AllenCahnBatch
+    a = [_solver(c, torch.float32) for c in CASES]
+    m = [_solver(c, torch.float32) for c in CASES]
+    ba, bm = AllenCahnBatch(a), AllenCahnBatch(m)
+    ba.run(3)
+    bm.run(3)
+    per, ms = bm.autotune(reps=2)
+    assert per in (1, 2, 4, 8, 16, 32) and ms > 0
+    ba.run(5)
+    bm.run(5)
+    for x, y in zip(a, m):
+        assert torch.equal(x.phi, y.phi) and torch.equal(x.u, y.u)
+
+
+def test_batch_measure_per_case():
+    from lbm.batch import AllenCahnBatch
+    m = [_solver(c, torch.float32) for c in CASES]
+    b = AllenCahnBatch(m)
+    b.run(10)
+    for s in m:
+        d = s.measure()
+        assert d["count"] > 0 and not d["has_nan"]
+        assert d["volume"] == pytest.approx(s.scalars()[0], rel=1e-2)

@@ -90,15 +90,23 @@ def test_steps_vs_reference_and_oracle(name, dn):
 
 @pytest.mark.parametrize("tile", [(4, 4, 8), (6, 5, 7), (12, 12, 28)])
 def test_results_independent_of_tiling(tile):
-    """The fused kernel's tile shape changes only the order of the per-tile
-    partial sums of phi (accumulated in float64)."""
+    """Tile shapes of the fused kernel give identical results (the sum of phi
+    is an exact fixed-point sum, independent of the order of the partial
+    sums); the fused kernel and the two-kernel step (the default) agree to a
+    few float32 ulps (the compiler contracts multiply-adds differently in
+    the two kernels)."""
     from lbm import _native as nat
     case, a = _gpu("ridge_l162", "float32")
     _, b = _gpu("ridge_l162", "float32")
+    _, c = _gpu("ridge_l162", "float32")
     nat.check(b._lib.lbm_set_tile(b._h, *tile), "lbm_set_tile")
+    nat.check(c._lib.lbm_set_tile(c._h, 5, 6, 9), "lbm_set_tile")
     a.run(20)
     b.run(20)
-    assert torch.equal(a.phi, b.phi) and torch.equal(a.u, b.u)
+    c.run(20)
+    assert torch.equal(b.phi, c.phi) and torch.equal(b.u, c.u)
+    assert (a.phi - b.phi).abs().max().item() <= 2e-6
+    assert rel_l2(_np(a.u), _np(b.u)) <= 1e-5
 
 
 @pytest.mark.parametrize("name", ["flat_q120_long", "ridge_l162_long"])
@@ -155,12 +163,21 @@ def test_measure_matches_oracle():
 
 
 def test_autotune_leaves_state_unchanged():
+    """The autotuner times candidates without advancing the state: the next
+    steps with its choice continue from the same state (bit-identical when
+    it keeps the two-kernel step, within a few ulps when it picks the fused
+    kernel)."""
     case, a = _gpu("ridge_l162", "float32")
     _, b = _gpu("ridge_l162", "float32")
     a.run(3)
     b.run(3)
+    assert torch.equal(a.phi, b.phi) and torch.equal(a.u, b.u)
     tile, ms = b.autotune(reps=2)
-    assert all(t >= 2 for t in tile) and ms > 0
+    assert (tile == (0, 0, 0) or all(t >= 2 for t in tile)) and ms > 0
+    assert b.scalars()[3] == a.scalars()[3]
     a.run(10)
     b.run(10)
-    assert torch.equal(a.phi, b.phi) and torch.equal(a.u, b.u)
+    if tile == (0, 0, 0):
+        assert torch.equal(a.phi, b.phi) and torch.equal(a.u, b.u)
+    else:
+        assert (a.phi - b.phi).abs().max().item() <= 2e-6
