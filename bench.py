@@ -330,6 +330,107 @@ def run_ours(args, rank, world, device):
     return out
 
 
+def _events_time(fn, device):
+    """Seconds of device time of fn() on the current stream (CUDA events)."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize(device)
+    return e0.elapsed_time(e1) / 1e3
+
+
+def run_sweep(args, device):
+    """The batched sweep: `--sweep-cases` seeded impact cases (grids
+    96^3 / 128x128x96 / 150x150x107 / 192x192x128, four substrates, R_d, theta,
+    u_z drawn per case) advanced `--sweep-steps` steps each.  Timed: the
+    batched half-precision form (one launch per kernel per step for all cases,
+    CUDA graph, autotuned phi kernel), the batched float32 form, and the plain
+    form (float32, one case at a time, each run to completion); device time
+    only, with the state resident.  Check: spread factor D/(2 R_d), aspect k and
+    volume of the first `--sweep-check` cases against float64 runs."""
+    import torch
+    from lbm.batch import AllenCahnBatch
+    from lbm.impact import SWEEP_GRIDS, build_impact_case, sample_impact_case
+    n_steps = args.sweep_steps
+    cases = [sample_impact_case(args.seed + i, SWEEP_GRIDS, (n_steps, n_steps)) for i in range(args.sweep_cases)]
+    updates = float(sum(c.nodes for c in cases)) * n_steps
+
+    def batched(dtype):
+        t = time.perf_counter()
+        solvers = [build_impact_case(c, dtype) for c in cases]
+        setup = time.perf_counter() - t
+        b = AllenCahnBatch(solvers)
+        b.run(1)
+        per, _ = b.autotune(reps=3)
+        secs = _events_time(lambda: b.run(n_steps - 1), device)
+        meas = [s.measure() for s in solvers[:args.sweep_check]]
+        b.close()
+        for s in solvers:
+            s.close()
+        return float(sum(c.nodes for c in cases)) * (n_steps - 1) / secs / 1e6, secs, setup, per, meas
+
+    m16, t16, set16, per16, meas16 = batched(torch.float16)
+    m32b, t32b, _, per32, meas32 = batched(torch.float32)
+    plain = 0.0
+    for c in cases:
+        s = build_impact_case(c, torch.float32)
+        s.run(1)
+        plain += _events_time(lambda: s.run(n_steps - 1), device)
+        s.close()
+    m32p = float(sum(c.nodes for c in cases)) * (n_steps - 1) / plain / 1e6
+    check = []
+    for c, a16, a32 in zip(cases[:args.sweep_check], meas16, meas32):
+        s = build_impact_case(c, torch.float64)
+        s.run(n_steps)
+        m = s.measure()
+        s.close()
+        beta = lambda d: max(d["Dx"], d["Dy"]) / (2.0 * c.R_d)
+        check.append({"case": c.seed, "grid": list(c.grid), "substrate": c.substrate,
+                      "beta_f64": beta(m), "beta_f16": beta(a16), "beta_f32": beta(a32),
+                      "k_f64": m["k"], "k_f16": a16["k"],
+                      "volume_rel_err_f16": abs(a16["volume"] - m["volume"]) / m["volume"],
+                      "beta_rel_err_f16": abs(beta(a16) - beta(m)) / beta(m)})
+    return {"metric": "MLUPS", "value": m16, "unit": "MLUPS", "n_gpus": 1, "steps": n_steps,
+            "higher_is_better": True, "dtype": "f16 storage / f32 math", "data": "synthetic",
+            "config": {"workload": f"batched sweep: {len(cases)} impact cases x {n_steps} steps, grids "
+                                   "96^3 / 128x128x96 / 150x150x107 / 192x192x128, flat/ridge/convex/concave, "
+                                   "R_d~U[15,30], theta~U[90,162], u_z~U[-0.08,-0.02], seeds "
+                                   f"{args.seed}..{args.seed + len(cases) - 1}",
+                       "node_updates": updates},
+            "batched_f16": {"mlups": m16, "seconds": t16, "setup_s": set16, "phi_nodes_per_thread": per16},
+            "batched_f32": {"mlups": m32b, "seconds": t32b, "phi_nodes_per_thread": per32},
+            "plain_f32": {"mlups": m32p, "seconds": plain, "what": "one case at a time, each to completion"},
+            "speedup_f16_batched_vs_plain_f32": m16 / m32p,
+            "fp64_check": check}
+
+
+def run_serve(args, device):
+    """The serving loop: `--serve-requests` impact requests (grids up to
+    256x256x192, steps U[1000, 4000]) with Poisson arrivals (4 per second),
+    admitted by HBM footprint within `--serve-budget-gb`; continuous batching
+    in half precision against the plain one-at-a-time float32 path on the
+    same request stream.  Wall-clock times include each case's set-up."""
+    import torch
+    from lbm.impact import SERVE_GRIDS, sample_impact_case
+    from lbm.serve import GpuBackend, Request, poisson_arrivals, serve, serve_sequential
+    arr = poisson_arrivals(args.serve_requests, 4.0, args.seed)
+    reqs = [Request(i, sample_impact_case(args.seed + 1000 + i, SERVE_GRIDS, (1000, 4000)), a)
+            for i, a in enumerate(arr)]
+    budget = int(args.serve_budget_gb * 1e9)
+    res_b, st_b = serve(reqs, GpuBackend(torch.float16), budget, tick=100, builders=4)
+    res_s, st_s = serve_sequential(reqs, GpuBackend(torch.float32))
+    return {"metric": "MLUPS", "value": st_b["mlups"], "unit": "MLUPS", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "f16 storage / f32 math", "data": "synthetic",
+            "config": {"workload": f"serving: {len(reqs)} impact requests, Poisson 4/s, grids up to 256x256x192, "
+                                   f"steps U[1000,4000], HBM budget {args.serve_budget_gb} GB",
+                       "node_updates": float(sum(r.case.nodes * r.case.steps for r in reqs))},
+            "served_f16_batched": st_b, "plain_f32_sequential": st_s,
+            "mlups_ratio": st_b["mlups"] / st_s["mlups"], "p99_ratio": st_b["p99_s"] / st_s["p99_s"]}
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -352,7 +453,13 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ridge150", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ridge150", choices=sorted(WORKLOADS) + ["serve", "sweep"])
+    ap.add_argument("--seed", type=int, default=0, help="first seed of the sweep / serving cases")
+    ap.add_argument("--sweep-cases", type=int, default=64)
+    ap.add_argument("--sweep-steps", type=int, default=1500)
+    ap.add_argument("--sweep-check", type=int, default=4, help="sweep cases also run in float64")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -372,6 +479,12 @@ def main():
     import torch
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
+    if args.workload in ("sweep", "serve"):
+        if world > 1:
+            raise SystemExit("the sweep and serving workloads run on one GPU")
+        out = run_sweep(args, device) if args.workload == "sweep" else run_serve(args, device)
+        print(json.dumps(out), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=device)

@@ -100,57 +100,78 @@ def _stats(results, wall):
             "mlups": updates / wall / 1e6 if wall > 0 else 0.0}
 
 
-def serve(requests, backend, budget_bytes, tick=100, max_slots=None, clock=time.perf_counter, sleep=time.sleep):
+def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0, clock=time.perf_counter,
+          sleep=time.sleep):
     """Continuous batching of `requests` under an HBM budget and at most
-    `max_slots` resident cases (None: no limit).  Returns (results in
-    completion order, stats)."""
+    `max_slots` resident cases (None: no limit).  With builders > 0, admitted
+    cases are set up (inputs, geometry, init) by that many host threads while
+    the GPU keeps stepping the resident ones; their footprint counts against
+    the budget from the start of the set-up.  Returns (results in completion
+    order, stats)."""
+    from concurrent.futures import ThreadPoolExecutor
     pending = sorted(requests, key=lambda r: r.arrival)
     for r in pending:
         if backend.footprint(r.case) > budget_bytes:
             raise ValueError(f"request {r.rid} needs more than the whole budget")
+    pool = ThreadPoolExecutor(max_workers=builders) if builders > 0 else None
+    building = {}      # rid -> (future, request, bytes)
     active = {}        # rid -> [request, solver, remaining steps, bytes, admitted]
     used = 0
     batch = None
     members = ()
     results = []
     t0 = clock()
-    while pending or active:
-        now = clock() - t0
-        # admit, in arrival order, what has arrived and fits
-        while (pending and pending[0].arrival <= now and used + backend.footprint(pending[0].case) <= budget_bytes
-               and (max_slots is None or len(active) < max_slots)):
-            r = pending.pop(0)
-            b = backend.footprint(r.case)
-            active[r.rid] = [r, backend.build(r.case), int(r.case.steps), b, clock() - t0]
-            used += b
-        if not active:
-            # idle until the next arrival
-            sleep(max(0.0, pending[0].arrival - (clock() - t0)))
-            continue
-        key = tuple(sorted(active))
-        if key != members:
-            if batch is not None:
+    try:
+        while pending or active or building:
+            now = clock() - t0
+            # admit, in arrival order, what has arrived and fits
+            while (pending and pending[0].arrival <= now
+                   and used + backend.footprint(pending[0].case) <= budget_bytes
+                   and (max_slots is None or len(active) + len(building) < max_slots)):
+                r = pending.pop(0)
+                b = backend.footprint(r.case)
+                used += b
+                if pool is None:
+                    active[r.rid] = [r, backend.build(r.case), int(r.case.steps), b, clock() - t0]
+                else:
+                    building[r.rid] = (pool.submit(backend.build, r.case), r, b)
+            for rid in [k for k, v in building.items() if v[0].done()]:
+                fut, r, b = building.pop(rid)
+                active[rid] = [r, fut.result(), int(r.case.steps), b, clock() - t0]
+            if not active:
+                if building:
+                    sleep(0.002)  # a set-up is in progress
+                else:
+                    sleep(max(0.0, pending[0].arrival - (clock() - t0)))  # idle until the next arrival
+                continue
+            key = tuple(sorted(active))
+            if key != members:
+                if batch is not None:
+                    batch.close()
+                batch = backend.batch([active[k][1] for k in key])
+                members = key
+            n = min(tick, min(a[2] for a in active.values()))
+            batch.run(n)
+            done = []
+            for k, a in active.items():
+                a[2] -= n
+                if a[2] == 0:
+                    done.append(k)
+            if done:
+                # retire: measuring waits for the batch's steps to finish
                 batch.close()
-            batch = backend.batch([active[k][1] for k in key])
-            members = key
-        n = min(tick, min(a[2] for a in active.values()))
-        batch.run(n)
-        done = []
-        for k, a in active.items():
-            a[2] -= n
-            if a[2] == 0:
-                done.append(k)
-        if done:
-            # retire: measuring waits for the batch's steps to finish
+                batch, members = None, ()
+                for k in done:
+                    r, solver, _, b, adm = active.pop(k)
+                    m, phi = backend.finish(solver)
+                    results.append(Result(r.rid, r.arrival, adm, clock() - t0, int(r.case.steps), r.case.nodes, m,
+                                          phi))
+                    used -= b
+    finally:
+        if batch is not None:
             batch.close()
-            batch, members = None, ()
-            for k in done:
-                r, solver, _, b, adm = active.pop(k)
-                m, phi = backend.finish(solver)
-                results.append(Result(r.rid, r.arrival, adm, clock() - t0, int(r.case.steps), r.case.nodes, m, phi))
-                used -= b
-    if batch is not None:
-        batch.close()
+        if pool is not None:
+            pool.shutdown(wait=True)
     backend.sync()
     return results, _stats(results, clock() - t0)
 

@@ -148,3 +148,12 @@ def test_slots_cap_the_number_of_resident_cases():
     res, _ = serve(reqs, be, 10 ** 12, tick=64, max_slots=2, clock=clk, sleep=clk.sleep)
     assert len(res) == len(reqs)
     assert max(k for _, k in be.ticks) <= 2
+
+
+def test_background_setup_serves_every_request():
+    clk = Clock()
+    be = FakeBackend(clk)
+    reqs = _requests()
+    res, st = serve(reqs, be, 10 ** 12, tick=64, builders=2, clock=clk, sleep=clk.sleep)
+    assert sorted(r.rid for r in res) == [r.rid for r in reqs]
+    assert all(r.measure["steps"] == r.steps for r in res)
