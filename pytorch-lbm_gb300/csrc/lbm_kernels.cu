@@ -422,8 +422,18 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   const size_t N = (size_t)k.N;
   const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
 
-  // loads that do not depend on the stencil first, so that their latency
-  // overlaps it: g (pulled), u and phi of the last step
+  // 2. first the stencil: gradient and laplacian with the ghost-node wetting values
+  T ps[Q];
+#pragma unroll
+  for (int q = 1; q < Q; ++q) ps[q] = phi_at(q);
+  T gx, gy, gz, lap;
+  grad_lap<T, true, State<T, S>, SolidAt, true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
+
+  // then g (pulled), u and phi of the last step.  Loading them after the
+  // stencil keeps the 18 stencil values and the 19 populations from being
+  // live at once (fewer registers, no spills; measured 157 -> 137 us per
+  // update launch on the 150x150x107 case; moving the density, chemical
+  // potential and wall correction ahead of these loads as well measured 143).
   const T eps = (c & kPartial) ? s.eps[n] : T(0);
   T g[Q];
   T uo0, uo1, uo2, pp;
@@ -453,13 +463,6 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     uo2 = ld_pol(s.u + (2 * Nu + nu), pol.once);
     pp = FIRST ? T(0) : ld_pol(s.phi_in + n, pol.once);
   }
-
-  // 2. gradient and laplacian with the ghost-node wetting values
-  T ps[Q];
-#pragma unroll
-  for (int q = 1; q < Q; ++q) ps[q] = phi_at(q);
-  T gx, gy, gz, lap;
-  grad_lap<T, true, State<T, S>, SolidAt, true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
 
   const T rho = fma_(phi, k.rho_l, (T(1) - phi) * k.rho_g);
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
