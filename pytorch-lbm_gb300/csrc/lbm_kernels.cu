@@ -16,14 +16,19 @@
 // without c and without relaxation.  Right after init (RAW) the buffers hold
 // the reference state itself.
 //
-// One step = ONE launch of k_step.  Each CTA owns a tile of nodes: phase A
-// recovers phi on the tile plus a one-node halo into shared memory (pulling
-// f), phase B runs the stencils, wetting, forces, velocity, Allen-Cahn source
-// and both BGK collisions for the tile's nodes (pulling f again, from L1/L2,
-// and g).  The grid-wide sum of phi that gives the next mass correction is a
-// deterministic last-block reduction of the per-tile partial sums.
-// Arithmetic follows the reference's operation order; sums run in population
-// order; the isotropic gradient is accumulated without FMA contraction.
+// One step = two launches (k_phi_batch, k_update_batch; the first step after
+// init: k_phi, k_update).  k_phi recovers phi of every node (pulling f) into
+// the phi buffer and reduces the grid's sum of phi, an exact fixed-point sum,
+// into the next mass-correction factor; k_update reads the phi stencil from
+// L2 and runs the stencils, wetting, forces, velocity, Allen-Cahn source and
+// both BGK collisions of every node (pulling g).  The batched kernels serve
+// many grids per launch through a case table and single grids through a
+// one-entry table.  An alternative fused kernel (k_step) does a whole step in
+// one launch per tile of nodes, recomputing phi on a one-node halo in shared
+// memory.  Arithmetic follows the reference's operation order where it
+// matters for parity; the isotropic gradient is accumulated without FMA
+// contraction.  (Measured and dropped for k_phi: runs of four consecutive
+// nodes per thread -- 43 -> 58 us, the per-thread runs break coalescing.)
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
