@@ -1010,6 +1010,15 @@ struct CaseDesc {
   int upd_blk0, upd_nblk;  // and in the k_update_batch grid
 };
 
+// Programmatic dependent launch between the step kernels: a kernel launched
+// with the programmatic-serialization attribute may start while the kernel
+// before it drains; it reads its descriptor, lets the next kernel be
+// scheduled (each block triggers on entry, so the next grid starts during
+// this grid's last wave), and waits for the previous grid to complete and
+// flush its memory before it reads anything that grid wrote.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <typename D>
 __device__ __forceinline__ void load_desc(D& dst, const D* src) {
   static_assert(sizeof(D) % 4 == 0, "descriptor copied as 32-bit words");
@@ -1024,6 +1033,8 @@ __global__ void __launch_bounds__(kBlock) k_phi_batch(const CaseDesc<T, S>* __re
                                                      const unsigned short* __restrict__ blk2case) {
   __shared__ CaseDesc<T, S> d;
   load_desc(d, cases + (blk2case ? blk2case[blockIdx.x] : 0));
+  pdl_trigger();
+  pdl_wait();  // f of the previous update kernel
   const Pol pol = Pol::make();
   const int b = blockIdx.x - d.phi_blk0, nb = d.phi_nblk;
   TileSum<T> part;
@@ -1036,6 +1047,8 @@ __global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_updat
     const CaseDesc<T, S>* __restrict__ cases, const unsigned short* __restrict__ blk2case) {
   __shared__ CaseDesc<T, S> d;
   load_desc(d, cases + (blk2case ? blk2case[blockIdx.x] : 0));
+  pdl_trigger();
+  pdl_wait();  // phi of the phi kernel
   const int n = (blockIdx.x - d.upd_blk0) * kBlock + threadIdx.x;
   if (n < d.k.N) update_one<T, S, false, false, OMEGA1>(d.k, d.s, n, Pol::make());
 }
@@ -1348,23 +1361,36 @@ cudaError_t launch_step(const Consts<T>& k, const State<T, S>& s, const Tiling& 
              : launch_step_t<T, S, false, false, false>(k, s, tl, st);
 }
 
-// Batched step kernels over a device case table; phi_blocks / upd_blocks:
-// total blocks of the two grids (the lengths of the block -> case tables).
+// Launch with programmatic stream serialization (see pdl_wait).
+constexpr int kPdlOn = 1;  // 0: plain stream serialization
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*fn)(KArgs...), int blocks, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = kPdlOn;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fn, args...);
+}
+
+// Batched step kernels over a device case table; blocks: the grid (the
+// length of the block -> case table).
 template <typename T, typename S>
 cudaError_t launch_phi_batch(const void* cases, const unsigned short* b2c, int blocks, cudaStream_t st) {
   if (blocks <= 0) return cudaSuccess;
-  k_phi_batch<T, S><<<blocks, kBlock, 0, st>>>(static_cast<const CaseDesc<T, S>*>(cases), b2c);
-  return cudaGetLastError();
+  return launch_pdl(k_phi_batch<T, S>, blocks, st, static_cast<const CaseDesc<T, S>*>(cases), b2c);
 }
 template <typename T, typename S>
 cudaError_t launch_update_batch(const void* cases, const unsigned short* b2c, int blocks, bool omega1,
                                 cudaStream_t st) {
   if (blocks <= 0) return cudaSuccess;
-  if (omega1)
-    k_update_batch<T, S, true><<<blocks, kBlock, 0, st>>>(static_cast<const CaseDesc<T, S>*>(cases), b2c);
-  else
-    k_update_batch<T, S, false><<<blocks, kBlock, 0, st>>>(static_cast<const CaseDesc<T, S>*>(cases), b2c);
-  return cudaGetLastError();
+  if (omega1) return launch_pdl(k_update_batch<T, S, true>, blocks, st, static_cast<const CaseDesc<T, S>*>(cases), b2c);
+  return launch_pdl(k_update_batch<T, S, false>, blocks, st, static_cast<const CaseDesc<T, S>*>(cases), b2c);
 }
 template <typename T, typename S>
 size_t case_desc_bytes() {
