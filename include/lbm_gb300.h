@@ -155,6 +155,21 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u,
  * lbm/fe_ac_solver.py:97-98). */
 int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream);
 
+/* Inject a droplet mid-run: centre (3 doubles, lattice units), radius,
+ * interface width xi, impact velocity (3 doubles, NULL = zero).  As the
+ * reference: phi becomes max(phi, C) where the droplet profile
+ * C = 0.5 + 0.5 tanh(2 (R - |x - centre|) / xi) exceeds 0.1 (its core), u
+ * becomes (1 - C) u + C u_impact everywhere, f and g are reset to their
+ * equilibria (with the last step's pressure P) at the core nodes, solid
+ * nodes keep phi = 0 and u = 0, the phi-mass reference becomes the new sum of
+ * phi, and the next step has no previous phi u.  Until the next step the
+ * fields read as after init_fields (P = 0, p = rho cs^2, the init laplacian
+ * in mu_phi), where the reference keeps its last P and mu_phi.  core_nodes
+ * (may be NULL; if given the call synchronises `stream`): the number of core
+ * nodes.  Replaces AllenCahnSolver.inject_droplet (lbm/fe_ac_solver.py:645-732). */
+int lbm_inject_droplet(LbmHandle* h, const double* center3, double radius, double xi, const double* u_impact3,
+                       int64_t* core_nodes, void* stream);
+
 /* Geometry tables as computed by lbm_set_geometry, into host buffers (any may
  * be NULL): node class byte (N), is_boundary (N), wall_normal (3N float32),
  * wall_weight (N float32), near_wall mask (N), partial mask (N).  Mirrors

@@ -373,6 +373,38 @@ class OracleSolver:
         s = self.w_view * (eu_cs2 + eu_cs2 * eu_cs2 / 2.0 - u_sq[None] / (2.0 * CS2))
         return P[None] * self.w_view + s
 
+    # -- mid-run droplet injection (lbm/fe_ac_solver.py:645-732) ----------
+    def inject_droplet(self, center, radius, xi, u_impact=None):
+        """Blend a new droplet into phi (max inside its core C > 0.1), blend
+        u towards u_impact with weight C everywhere, reset f and g to their
+        equilibria (with the current P) at the core nodes, re-base the phi
+        mass and drop the previous phi u."""
+        T = self.T
+        if u_impact is None:
+            u_impact = (0.0, 0.0, 0.0)
+        mesh = np.meshgrid(*[np.arange(n) for n in self.shape], indexing="ij")
+        dist = np.sqrt(sum((M - center[d]) ** 2 for d, M in enumerate(mesh)))
+        C = np.clip(0.5 + 0.5 * np.tanh(2.0 * (radius - dist) / xi), 0.0, 1.0).astype(np.float32).astype(T)
+        core = C > T(0.1)
+        phi = np.where(core, np.maximum(self.phi, C), self.phi)
+        phi = np.clip(phi, T(0), T(1))
+        if self.solid_any:
+            phi = np.where(self.solid, T(0), phi)
+        self.phi = phi.astype(T)
+        self.rho = self.phi * self.cfg.rho_l + (1.0 - self.phi) * self.cfg.rho_g
+        u_new = np.stack([np.full(self.shape, u_impact[d], dtype=T) for d in range(3)])
+        u = (T(1) - C)[None] * self.u + C[None] * u_new
+        if self.solid_any:
+            u = np.where(self.solid[None], T(0), u)
+        self.u = u.astype(T)
+        f_eq = self._f_eq(self.phi, self.u)
+        g_eq = self._g_eq(self.P, self.u)
+        self.f = np.where(core[None], f_eq, self.f).astype(T)
+        self.g = np.where(core[None], g_eq, self.g).astype(T)
+        self.phi_mass_init = float(T(self.phi.astype(np.float64).sum()))
+        self.phi_u_prev = None
+        return int(core.sum())
+
     # -- the time step (lbm/fe_ac_solver.py:380-639) -----------------------
     def step(self):
         T = self.T

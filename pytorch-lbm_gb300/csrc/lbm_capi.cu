@@ -29,6 +29,9 @@ cudaError_t launch_observe(const Consts<T>&, const State<T, S>&, bool, unsigned,
                            cudaStream_t);
 template <typename T, typename S>
 cudaError_t launch_populations(const Consts<T>&, const State<T, S>&, bool, T*, T*, cudaStream_t);
+template <typename T, typename S>
+cudaError_t launch_inject(const Consts<T>&, const State<T, S>&, bool, const InjectParams&, const T*, unsigned*,
+                          cudaStream_t);
 template <typename T>
 cudaError_t launch_measure(int, int, int, const T*, const uint8_t*, double*, int, unsigned*, double*,
                            cudaStream_t);
@@ -99,6 +102,7 @@ struct LbmHandle {
   int c_last = 0;         // cbuf slot of the last step's correction
   int64_t steps = 0;
   bool last_raw_in = true;  // mode of the last step's input (for P read-out)
+  bool obs_init = true;     // fields read as after init_fields (no step since init or an injection)
   // the two-kernel step runs the batched kernels on a one-case table: device
   // descriptors for the two step parities, valid while desc_ok
   void* desc = nullptr;
@@ -362,6 +366,7 @@ int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr
     const int rc = launch_next<T, S>(h, h->tiling, st, ev ? ev[2 * i + 1] : nullptr);
     if (rc != LBM_OK) return rc;
     h->last_raw_in = h->raw;
+    h->obs_init = false;
     h->cur ^= 1;
     h->pc ^= 1;
     h->c_last ^= 1;
@@ -575,6 +580,7 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
   h->c_last = 0;
   h->steps = 0;
   h->last_raw_in = true;
+  h->obs_init = true;
   return LBM_OK;
 }
 
@@ -720,8 +726,8 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u, v
       ((mask & LBM_FIELD_P) && !P) || ((mask & LBM_FIELD_PRESS) && !p) || ((mask & LBM_FIELD_MU) && !mu))
     return fail(LBM_E_ARG, "lbm_get_fields: selected output is null");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int mode = h->steps == 0 ? 0 : 1;
-  const int in_buf = h->steps == 0 ? h->cur : (h->cur ^ 1);  // the last step's input buffer
+  const int mode = h->obs_init ? 0 : 1;
+  const int in_buf = h->obs_init ? h->cur : (h->cur ^ 1);  // the last step's input buffer
   cudaError_t e;
   // phi_out of the state = the latest recovered phi
   e = with_types(h->prec, [&](auto tag) {
@@ -733,6 +739,57 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u, v
                                 (T*)P, (T*)p, (T*)mu, st);
   });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_get_fields: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+int lbm_inject_droplet(LbmHandle* h, const double* center3, double radius, double xi, const double* u_impact3,
+                       int64_t* core_nodes, void* stream) {
+  if (!h || !center3) return fail(LBM_E_ARG, "lbm_inject_droplet: null argument");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_inject_droplet: call lbm_init_fields first");
+  if (!(radius >= 0.0) || !(xi > 0.0)) return fail(LBM_E_ARG, "lbm_inject_droplet: radius >= 0 and xi > 0 required");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  InjectParams ip;
+  std::memset(&ip, 0, sizeof(ip));
+  for (int d = 0; d < 3; ++d) {
+    ip.c[d] = center3[d];
+    ip.u[d] = u_impact3 ? u_impact3[d] : 0.0;
+  }
+  ip.radius = radius;
+  ip.xi = xi;
+  ip.obs_init = h->obs_init ? 1 : 0;
+  CUDA_TRY(cudaMemsetAsync(h->counters + 3, 0, sizeof(unsigned), st));
+  cudaError_t e = with_types(h->prec, [&](auto tag) {
+    using T = typename decltype(tag)::T;
+    using S = typename decltype(tag)::S;
+    const Consts<T>& k = consts_of<T>(*h);
+    cudaError_t r = cudaSuccess;
+    if (!h->obs_init) {
+      // the P attribute: the pressure of the last step, into the measure scratch
+      State<T, S> so = make_state<T, S>(*h, h->cur ^ 1, h->pc ^ 1);
+      so.c_cur = h->c_last;
+      r = launch_observe<T, S>(k, so, h->last_raw_in, LBM_FIELD_P, 1, nullptr, nullptr, nullptr,
+                               static_cast<T*>(h->meas_phi), nullptr, nullptr, st);
+      if (r != cudaSuccess) return r;
+    }
+    State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
+    s.c_prev = h->c_last;
+    return launch_inject<T, S>(k, s, h->raw, ip, static_cast<const T*>(h->meas_phi), h->counters + 3, st);
+  });
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_inject_droplet: ") + cudaGetErrorString(e));
+  // the injected state is raw (read in place) and has no previous phi u
+  h->cur ^= 1;
+  h->pc ^= 1;
+  h->raw = true;
+  h->first = true;
+  h->obs_init = true;
+  h->last_raw_in = true;
+  h->desc_ok = false;
+  if (core_nodes) {
+    unsigned cnt = 0;
+    CUDA_TRY(cudaMemcpyAsync(&cnt, h->counters + 3, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    *core_nodes = cnt;
+  }
   return LBM_OK;
 }
 
@@ -991,6 +1048,7 @@ void batch_advance(LbmBatch* b, int nsteps) {
     }
     h->steps += nsteps;
     h->last_raw_in = false;
+    h->obs_init = false;
   }
 }
 

@@ -168,6 +168,14 @@ struct State {
   int c_prev, c_cur;  // cbuf slots: factor applied to fin, factor produced this step
 };
 
+// Droplet to inject mid-run (lbm/fe_ac_solver.py:645-732): centre, radius,
+// interface width, impact velocity; obs_init: the attributes phi, u, P are
+// those of init_fields (no step since init or the last injection).
+struct InjectParams {
+  double c[3], radius, xi, u[3];
+  int obs_init;
+};
+
 // Tiling of the fused step kernel: one CTA per tile of TX x TY x TZ nodes
 // (z fastest), tiles clipped at the domain edge.
 struct Tiling {

@@ -1116,6 +1116,94 @@ __global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T, S> s, con
 }
 
 // ---------------------------------------------------------------------------
+// Mid-run droplet injection (lbm/fe_ac_solver.py:645-732).  Reads the state
+// the reference holds between steps (populations as k_populations rebuilds
+// them, phi / u / P as the attributes), blends the new droplet in and writes
+// the result in the raw form init_fields leaves (populations as the reference
+// holds them): f, g to the other population buffer, phi to the other phi
+// buffer, u in place.  Sums the new phi (the new phi-mass reference) and
+// counts the core nodes.
+// ---------------------------------------------------------------------------
+template <typename T, typename S, bool RAW>
+__global__ void __launch_bounds__(kBlock) k_inject(Consts<T> k, State<T, S> s, InjectParams ip,
+                                                   const T* __restrict__ P_attr, unsigned* core_count) {
+  using IO = PopIO<T, S>;
+  const int n = blockIdx.x * kBlock + threadIdx.x;
+  double part = 0.0;
+  bool core = false;
+  if (n < k.N) {
+    const size_t N = (size_t)k.N;
+    const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+    const uint8_t c = s.cls[n];
+    int ix, iy, iz;
+    const Nbr nb = make_nbr(n, k.nx, k.ny, k.nz, &ix, &iy, &iz);
+    // the droplet as the reference builds it: float64 profile, stored as float32
+    const double dx = ix - ip.c[0], dy = iy - ip.c[1], dz = iz - ip.c[2];
+    const double dist = sqrt((dx * dx + dy * dy) + dz * dz);
+    double Cd = 0.5 + 0.5 * tanh(2.0 * (ip.radius - dist) / ip.xi);
+    Cd = Cd < 0.0 ? 0.0 : (Cd > 1.0 ? 1.0 : Cd);
+    const T C = (T)(float)Cd;
+    core = C > T(0.1);
+    // the attributes phi, u, P the reference holds now
+    const T corr = s.cbuf[s.c_prev];
+    T phi = s.phi_in[n];
+    if (!ip.obs_init) {
+      const T pr = phi;
+      phi = clamp01(pr * corr);
+      if (k.relax_on && (c & kTop)) {
+        const T r = relax_target(k, pr, corr);
+        if (r >= T(0)) phi = r;
+      }
+    }
+    T u[3] = {s.u[nu], s.u[Nu + nu], s.u[2 * Nu + nu]};
+    const T P = ip.obs_init ? T(0) : P_attr[n];
+    // the populations the reference holds now
+    const T eps = (c & kPartial) ? s.eps[n] : T(0);
+    T fv[Q], gv[Q];
+    fetch_f<T, S, RAW>(fv, k, s, n, N, nb, c, eps);
+    fetch_pop<T, S, RAW, false, false>(gv, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
+    // new phi: the maximum with the droplet in its core, clamped, zero in solid
+    T pn = core ? (phi > C ? phi : C) : phi;
+    pn = clamp01(pn);
+    if (c & kSolid) pn = T(0);
+    // new u: (1 - C) u + C u_impact everywhere, zero in solid
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      u[d] = add_rn(mul_rn(T(1) - C, u[d]), mul_rn(C, (T)ip.u[d]));
+      if (c & kSolid) u[d] = T(0);
+    }
+    if (core) {
+      const T b = ((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]) / k.two_cs2;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const T ec = edot(q, u[0], u[1], u[2]) / k.cs2;
+        fv[q] = pn * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b));
+        gv[q] = P * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b);
+      }
+    }
+    // raw form: the next step reads these in place (deviation reference: own phi)
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      s.fout[q * Nu + nu] = IO::st_f(fv[q], q, pn, k);
+      s.gout[q * Nu + nu] = IO::st_g(gv[q], q, k);
+    }
+    s.u[nu] = u[0];
+    s.u[Nu + nu] = u[1];
+    s.u[2 * Nu + nu] = u[2];
+    s.phi_out[n] = pn;
+    part = (double)pn;
+  }
+  const int cnt = __syncthreads_count(core);
+  if (threadIdx.x == 0 && cnt) atomicAdd(core_count, (unsigned)cnt);
+  part = block_sum(part);
+  double total;
+  if (last_block_total(part, s.partials, s.counter, &total)) {
+    s.scal[0] = (double)(T)total;  // phi_mass_init = phi.sum().item() in T
+    s.scal[1] = total;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Field read-out (the reference's attribute values after the last step).
 // s.phi_out holds the last recovered phi, s.cbuf[s.c_cur] its correction.
 // ---------------------------------------------------------------------------
@@ -1411,6 +1499,17 @@ void fill_case_desc(void* dst, const Consts<T>& k, const State<T, S>& s, int phi
   std::memcpy(dst, &d, sizeof(d));
 }
 
+template <typename T, typename S>
+cudaError_t launch_inject(const Consts<T>& k, const State<T, S>& s, bool raw, const InjectParams& ip,
+                          const T* P_attr, unsigned* core_count, cudaStream_t st) {
+  const int grid = (k.N + kBlock - 1) / kBlock;
+  if (raw)
+    k_inject<T, S, true><<<grid, kBlock, 0, st>>>(k, s, ip, P_attr, core_count);
+  else
+    k_inject<T, S, false><<<grid, kBlock, 0, st>>>(k, s, ip, P_attr, core_count);
+  return cudaGetLastError();
+}
+
 template <typename T, typename S, typename Src>
 cudaError_t launch_init(const Consts<T>& k, const State<T, S>& s, const Src* phi0, const Src* u0, cudaStream_t st) {
   const int grid = (k.N + kBlock - 1) / kBlock;
@@ -1524,7 +1623,9 @@ template size_t step_smem_bytes<float, __half>(const Tiling&);
                                                  const double*, cudaStream_t);                                    \
   template cudaError_t launch_observe<T, S>(const Consts<T>&, const State<T, S>&, bool, unsigned, int, T*, T*, T*, \
                                             T*, T*, T*, cudaStream_t);                                           \
-  template cudaError_t launch_populations<T, S>(const Consts<T>&, const State<T, S>&, bool, T*, T*, cudaStream_t);
+  template cudaError_t launch_populations<T, S>(const Consts<T>&, const State<T, S>&, bool, T*, T*, cudaStream_t);  \
+  template cudaError_t launch_inject<T, S>(const Consts<T>&, const State<T, S>&, bool, const InjectParams&,        \
+                                           const T*, unsigned*, cudaStream_t);
 
 LBM_INSTANTIATE(float, float)
 LBM_INSTANTIATE(double, double)

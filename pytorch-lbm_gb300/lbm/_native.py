@@ -25,6 +25,7 @@ EXPORTS = (
     "lbm_get_scalars", "lbm_measure", "lbm_status", "lbm_last_error", "lbm_version",
     "lbm_set_tile", "lbm_get_tile", "lbm_autotune", "lbm_measure_static", "lbm_footprint",
     "lbm_batch_create", "lbm_batch_step", "lbm_batch_size", "lbm_batch_autotune", "lbm_batch_destroy",
+    "lbm_inject_droplet",
 )
 
 
@@ -70,6 +71,8 @@ def _declare(L):
         "lbm_batch_size": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),
         "lbm_batch_autotune": ([_vp, _i32, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)], _i32),
         "lbm_batch_destroy": ([_vp], _i32),
+        "lbm_inject_droplet": ([_vp, ctypes.POINTER(_dbl), _dbl, _dbl, ctypes.POINTER(_dbl), ctypes.POINTER(_i64),
+                                _vp], _i32),
         "lbm_status": ([_vp, ctypes.POINTER(_u32)], _i32),
         "lbm_set_tile": ([_vp, _i32, _i32, _i32], _i32),
         "lbm_get_tile": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),

@@ -279,6 +279,27 @@ class AllenCahnSolver:
         self.t += float(nsteps)
         self._cache.clear()
 
+    # -- mid-run droplet injection --------------------------------------------
+    def inject_droplet(self, center, radius, xi, u_impact=None):
+        """Inject a droplet at the current time step (lbm/fe_ac_solver.py:645-732):
+        phi = max(phi, C) in the droplet core (C > 0.1), u blended towards
+        ``u_impact`` with weight C, f and g reset to equilibrium at the core
+        nodes, the phi-mass reference re-based, no previous phi u."""
+        if not self._initialized:
+            raise RuntimeError("init_fields must be called before inject_droplet()")
+        if u_impact is None:
+            u_impact = (0.0,) * 3
+        c = (ctypes.c_double * 3)(*[float(x) for x in center])
+        uv = (ctypes.c_double * 3)(*[float(x) for x in u_impact])
+        core = ctypes.c_int64()
+        nat.check(self._lib.lbm_inject_droplet(self._h, c, float(radius), float(xi), uv, ctypes.byref(core),
+                                               nat.stream_ptr()), "lbm_inject_droplet")
+        self._cache.clear()
+        center_str = ",".join(f"{x:.0f}" for x in center)
+        vel_str = ",".join(f"{x:.3f}" for x in u_impact)
+        print(f"  [inject] Droplet at ({center_str}) R={radius:.1f} u=({vel_str}) core_nodes={core.value}")
+        return int(core.value)
+
     # -- fields ---------------------------------------------------------------
     def _fields(self, want):
         missing = [k for k in want if k not in self._cache]

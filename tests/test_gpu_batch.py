@@ -87,3 +87,23 @@ def test_batch_measure_per_case():
         d = s.measure()
         assert d["count"] > 0 and not d["has_nan"]
         assert d["volume"] == pytest.approx(s.scalars()[0], rel=1e-2)
+
+
+def test_injected_case_in_batch_matches_alone():
+    """A case injected between batch calls continues bit-identically to the
+    same case stepped alone."""
+    from lbm.batch import AllenCahnBatch
+    a = [_solver(c, torch.float32) for c in CASES[:3]]
+    m = [_solver(c, torch.float32) for c in CASES[:3]]
+    for s in a:
+        s.run(4)
+    b = AllenCahnBatch(m)
+    b.run(4)
+    for s in (a[1], m[1]):
+        s.inject_droplet((16.0, 14.0, 19.0), 4.0, 4.0, u_impact=(0.0, 0.01, -0.02))
+    for s in a:
+        s.run(5)
+    b.run(5)
+    for x, y in zip(a, m):
+        for p, q in zip(_state(x), _state(y)):
+            assert torch.equal(p, q)

@@ -75,3 +75,40 @@ def test_long_runs_match_reference(name):
     assert np.abs(s.phi - gd[f"s{n}_phi"]).max() <= tp
     assert rel_l2(s.u, gd[f"s{n}_u"]) <= tu
     np.testing.assert_allclose(masses, gd["mass_every"], rtol=1e-6)
+
+
+@pytest.mark.parametrize("dn", ["float32", "float64"])
+def test_inject_droplet_matches_reference(dn):
+    """Mid-run droplet injection (lbm/fe_ac_solver.py:645-732) against the
+    reference's own outputs (tests/golden/make_golden_inject.py)."""
+    import os
+    from make_golden_inject import INJECT_CASE as case
+    from _cases import GOLDEN
+    gd = np.load(os.path.join(GOLDEN, f"inject_ridge_{dn}.npz"))
+    solid, frac, C, u = inputs(case)
+    s = OracleSolver(config(case), dtype=np.dtype(dn), **case["kw"])
+    s.set_solid(solid, frac)
+    s.init_fields(C, u)
+    for _ in range(case["before"]):
+        s.step()
+    inj = case["inject"]
+    s.inject_droplet(inj["center"], inj["radius"], inj["xi"], u_impact=inj["u_impact"])
+    tp = 3e-6 if dn == "float32" else 1e-13
+    assert np.abs(s.phi - gd["inj_phi"]).max() <= tp
+    assert rel_l2(s.u, gd["inj_u"]) <= (1e-5 if dn == "float32" else 1e-12)
+    if "inj_f" in gd:
+        assert np.abs(s.f - gd["inj_f"]).max() <= 5e-7
+        assert np.abs(s.g - gd["inj_g"]).max() <= 5e-7
+    assert s.phi_mass_init == pytest.approx(float(gd["inj_phi_mass_init"]), rel=1e-6 if dn == "float32" else 1e-12)
+    # The steps after the injection amplify rounding differences strongly: the
+    # max-blend of two overlapping droplets leaves a line inside the interface
+    # where the lattice gradient nearly cancels, so the sharpening direction
+    # grad phi / |grad phi| there is set by rounding (the reference against
+    # itself shows the same).  Pointwise bounds after 4 steps are therefore
+    # looser than the injection's own, and the phi mass is checked too.
+    for _ in range(case["after"]):
+        s.step()
+    assert np.abs(s.phi - gd["after_phi"]).max() <= (2e-4 if dn == "float32" else 1e-9)
+    assert rel_l2(s.u, gd["after_u"]) <= (1e-3 if dn == "float32" else 1e-8)
+    assert float(s.phi.astype(np.float64).sum()) == pytest.approx(float(gd["after_phi"].astype(np.float64).sum()),
+                                                                  rel=1e-6)
