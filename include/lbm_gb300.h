@@ -49,6 +49,10 @@ extern "C" {
 #define LBM_STAB_LIANG 1    /* F = F_s + F_p + F_body                         */
 #define LBM_STAB_NONE 2     /* F = F_s + F_body                               */
 
+/* interface_mode values (lbm/fe_ac_solver.py:76, 457-486). */
+#define LBM_IFACE_ALLEN_CAHN 0      /* conservative Allen-Cahn sharpening source   */
+#define LBM_IFACE_CAHN_HILLIARD 1   /* source M (grad mu - grad phi) tau/(tau-1/2) */
+
 /* Field selection bits for lbm_get_fields. */
 #define LBM_FIELD_PHI 1u
 #define LBM_FIELD_RHO 2u
@@ -79,13 +83,20 @@ typedef struct LbmParams {
     double ghost_scale;           /* <= 0: automatic (3 if |theta-90|>60 else 2) */
     int32_t stab_mode;            /* LBM_STAB_*                               */
     int32_t geometric_wetting;    /* 0/1                                      */
+    int32_t interface_mode;       /* LBM_IFACE_*; default Allen-Cahn          */
+    int32_t direct_wetting;       /* 0/1: cubic-wall-energy boundary phi      */
+    double mu_drive;              /* >= 0; default 0 (Allen-Cahn mode only)   */
 } LbmParams;
 
 typedef struct LbmHandle LbmHandle;
 
 /* Allocate the device state of one nx*ny*nz grid on the current CUDA device.
  * Replaces AllenCahnSolver.__init__ (lbm/fe_ac_solver.py:54-191).
- * Only 3-D grids (nz > 1) are supported. */
+ * Only 3-D grids (nz > 1) are supported.  The interface sources that need
+ * the gradient of the chemical potential (interface_mode Cahn-Hilliard,
+ * mu_drive > 0) add a chemical-potential pass to every step, run on LBM_F32
+ * and LBM_F64 grids (LBM_E_UNSUPPORTED with LBM_F16), with the two-kernel
+ * step only (no fused tile kernel) and one grid at a time (not in batches). */
 int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz,
                int precision, LbmHandle** out);
 
@@ -102,6 +113,17 @@ int lbm_destroy(LbmHandle* h);
  * _precompute_* (lbm/fe_wetting.py:39-367).  Synchronous. */
 int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction,
                      int fraction_dtype);
+
+/* Per-node geometric amplification field alpha (host, N elements of
+ * alpha_dtype, LBM_DT_F32 or LBM_DT_F64), used in place of the scalar
+ * params.geo_amplification: at each wetting boundary node the contact-angle
+ * correction is amplified by that node's alpha where alpha > 1 and left
+ * un-amplified elsewhere.  The field is rounded to the compute type, as the
+ * reference casts it.  alpha = NULL (with LBM_DT_NONE) returns to the scalar.
+ * Allocates N compute-type elements on the device (not counted by
+ * lbm_footprint); synchronises the device.  Replaces a tensor-valued
+ * geo_amplification (lbm/fe_wetting.py:501-512, lbm/fe_ac_solver.py:83). */
+int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype);
 
 /* Initial phase field phi (N elements) and optional velocity u (3N elements,
  * NULL = zero), of element type src_dtype, in host memory (on_device = 0) or
@@ -232,6 +254,30 @@ int lbm_measure(LbmHandle* h, double* out9, void* stream);
 int lbm_measure_static(int64_t nx, int64_t ny, int64_t nz, const void* phi, int phi_dtype,
                        const uint8_t* solid, double* out9, void* stream);
 
+/*
+ * Checkpoints.  A state blob holds everything the next step and the field
+ * read-outs depend on: the current populations (the library's own pull-form
+ * encoding), u, both phi buffers, the mass-correction factors, phi_mass_init
+ * and the last sum of phi, the step count, the status flags and the step
+ * sequencing flags.  It does not hold the configuration or the geometry: a
+ * blob is loaded into a handle created with the same parameters, grid and
+ * precision whose geometry was set from the same solid mask and fraction
+ * (checked through a hash of the node-class table).  A run resumed from a blob
+ * gives bit-identical results to the run that wrote it.  No reference
+ * counterpart (the reference has no state checkpoint; its sweep drivers save
+ * phi/u/solid snapshots, scripts/run_thesis_sweep.py:219-243).
+ */
+/* Size in bytes of the handle's state blob. */
+int lbm_state_bytes(LbmHandle* h, int64_t* bytes);
+
+/* Copy the state into a host buffer of exactly lbm_state_bytes bytes;
+ * synchronises `stream`. */
+int lbm_save_state(LbmHandle* h, void* host, int64_t bytes, void* stream);
+
+/* Restore a state written by lbm_save_state (LBM_E_ARG if it belongs to another
+ * grid, precision or geometry, or is not a state blob); synchronises `stream`. */
+int lbm_load_state(LbmHandle* h, const void* host, int64_t bytes, void* stream);
+
 /* Sticky status flags (LBM_STATUS_*) accumulated by the device; synchronises. */
 int lbm_status(LbmHandle* h, uint32_t* flags);
 
@@ -273,6 +319,16 @@ int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread
 
 /* Free the batch (not its handles). */
 int lbm_batch_destroy(LbmBatch* b);
+
+/* Legacy-VTK ASCII output of one snapshot, byte for byte the file of the
+ * reference's write_vtk (io_utils/vtk_writer.py:10-86): `header` (the text up
+ * to and including the POINT_DATA line, formatted by the caller), then the
+ * density scalars, the velocity vectors and, if `solid` is not NULL, the solid
+ * flags, each "%.6e" (NaN printed "nan") in the order of the caller's arrays
+ * (npoints host values each; the reference writes C order, z fastest).  Host
+ * only, no GPU needed.  Returns LBM_E_ARG if the file cannot be written. */
+int lbm_write_vtk(const char* path, const char* header, int64_t npoints, const double* rho,
+                  const double* ux, const double* uy, const double* uz, const int32_t* solid);
 
 /* Message for the last error on the calling thread ("" if none). */
 const char* lbm_last_error(void);

@@ -159,6 +159,17 @@ class OracleWetting:
         self.wall_weight = ww
         self.near_wall_mask = (dist < 2.0 * XI_NEAR_WALL) & ~solid
 
+        # next-interior node of every boundary node, one step along the rounded
+        # wall normal (round half to even, clamped to the grid, not periodic),
+        # and whether it is fluid (fe_wetting.py:313-367)
+        bnd = np.argwhere(isb)
+        shift = np.rint(np.stack([wn[d][isb] for d in range(3)], axis=1)).astype(np.int64)
+        nsw = np.clip(bnd + shift, 0, np.array(shape) - 1)
+        self.bnd_flat = np.ravel_multi_index(bnd.T, shape)
+        self.nsw_flat = np.ravel_multi_index(nsw.T, shape)
+        self.nsw_is_fluid = ~solid.reshape(-1)[self.nsw_flat]
+        self.cubic_a = 6.0 * self.sigma * math.cos(math.radians(self.theta_deg)) / self.kappa
+
         # per-direction ghost masks and n.e_i in float32 (fe_wetting.py:221-240)
         self.ghost_mask = [None] * Q
         self.n_dot_e = [None] * Q
@@ -170,6 +181,26 @@ class OracleWetting:
                     nde = nde + wn[d] * np.float32(E[i, d])
                 self.ghost_mask[i] = m
                 self.n_dot_e[i] = nde
+
+    def cubic_boundary_phi(self, phi):
+        """Boundary phi from the cubic wall energy (fe_wetting.py:369-416):
+        the root of a phi_b^2 + (1 - a) phi_b - phi_nsw = 0 at boundary nodes
+        whose next-interior node is fluid and 0.01 < phi < 0.99."""
+        a = self.cubic_a
+        if self.bnd_flat.size == 0 or abs(a) < 1e-10:
+            return phi
+        T = phi.dtype.type
+        flat = phi.reshape(-1)
+        phi_nsw = flat[self.nsw_flat]
+        old = flat[self.bnd_flat].copy()
+        oma = 1.0 - a
+        disc = np.maximum(oma ** 2 + (4.0 * a) * phi_nsw, T(0))
+        pb = np.clip((-oma + np.sqrt(disc)) / (2.0 * a), T(0), T(1))
+        active = self.nsw_is_fluid & (old > 0.01) & (old < 0.99)
+        out = phi.copy()
+        of = out.reshape(-1)
+        of[self.bnd_flat[active]] = pb[active]
+        return out
 
     def correct_shifted(self, phi, phi_shifted, i):
         """fe_wetting.py:418-446."""
@@ -226,7 +257,8 @@ class OracleSolver:
 
     def __init__(self, cfg, dtype=np.float64, stab_mode='auto', boundary_relax=0.3,
                  ghost_scale=None, sharpen_reduce=0.8, mu_wall_scale=1.0,
-                 geometric_wetting=False, geo_amplification=1.0, ac_scale=1.0):
+                 geometric_wetting=False, geo_amplification=1.0, ac_scale=1.0,
+                 interface_mode='allen-cahn', mu_drive=0.0, direct_wetting=False):
         self.cfg = cfg
         self.T = np.dtype(dtype).type
         T = self.T
@@ -239,6 +271,9 @@ class OracleSolver:
         self.geometric_wetting = geometric_wetting
         self.geo_amplification = geo_amplification
         self.ac_scale = ac_scale
+        self.interface_mode = interface_mode
+        self.mu_drive = mu_drive
+        self.direct_wetting = direct_wetting
         self.rho_floor = 0.5 * cfg.rho_l
         self.w = W32.astype(T)
         self.w_view = self.w.reshape(Q, 1, 1, 1)
@@ -320,6 +355,21 @@ class OracleSolver:
                     grad[d] = grad[d] + (wi * T(E[i, d])) * ps
             lap = lap + (2.0 * wi) * diff
         return grad, lap
+
+    def _lattice_gradient(self, v):
+        """Unfused isotropic gradient with the ghost correction applied to v
+        itself (lbm/fe_ac_solver.py:267-280): per direction i, per axis d with
+        e_id != 0, grad_d += ((w_i e_id) v(x + e_i)) / cs2."""
+        T = self.T
+        grad = np.zeros((3,) + self.shape, dtype=T)
+        for i in range(1, Q):
+            vs = _shift_from(v, E[i])
+            if self.wetting is not None:
+                vs = self.wetting.correct_shifted(v, vs, i)
+            for d in range(3):
+                if E[i, d] != 0:
+                    grad[d] = grad[d] + ((self.w[i] * T(E[i, d])) * vs) / CS2
+        return grad
 
     def _lap_only(self, phi):
         """Unfused laplacian used by init_fields (lbm/fe_ac_solver.py:282-294):
@@ -477,7 +527,18 @@ class OracleSolver:
         sharp = CS2 * lam[None] * n * self.ac_scale
         if self.wetting is not None:
             sharp = sharp * (1.0 - self.sharpen_reduce * self.wetting.wall_weight.astype(T))[None]
-        src = d_phi_u + sharp
+        mobility = CS2 * (self.tau_f - 0.5)
+        if self.interface_mode == 'cahn-hilliard' or self.mu_drive > 0.0:
+            grad_mu = self._lattice_gradient(self.mu_phi)
+        if self.interface_mode == 'cahn-hilliard':
+            # lbm/fe_ac_solver.py:457-461
+            guo = self.tau_f / (self.tau_f - 0.5)
+            src = d_phi_u + mobility * (grad_mu - grad) * guo
+        else:
+            src = d_phi_u + sharp
+            if self.mu_drive > 0.0:
+                # lbm/fe_ac_solver.py:484-486
+                src = src + (self.mu_drive * mobility) * grad_mu
         ac_coeff = 1.0 - 0.5 / self.tau_f
         F_src = ac_coeff * self.w_view * self._eu(src) / CS2
         # 8. collisions
@@ -533,12 +594,17 @@ class OracleSolver:
             top = (nz_abs[m] / nmag[m]) > 0.5
             inside = (phi_b > 0.15) & (phi_b < 0.85)
             tgt = self.phi_wall_target
-            if tgt is not None and abs(tgt - 0.5) > 0.05:
+            if self.direct_wetting:
+                # lbm/fe_ac_solver.py:609-612
+                target = wt.cubic_boundary_phi(self.phi)[m]
+                active = inside & top
+            elif tgt is not None and abs(tgt - 0.5) > 0.05:
+                target = np.full_like(phi_b, T(tgt))
                 active = inside & top
             else:
                 active = np.zeros_like(phi_b, dtype=bool)
             if active.any():
-                pnew = phi_b[active] + self.boundary_relax * (T(tgt) - phi_b[active])
+                pnew = phi_b[active] + self.boundary_relax * (target[active] - phi_b[active])
                 pnew = np.clip(pnew, T(0), T(1))
                 phi_b[active] = pnew
                 self.phi[m] = phi_b

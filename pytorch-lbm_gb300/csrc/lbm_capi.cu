@@ -40,7 +40,9 @@ cudaError_t launch_measure_static(int, int, int, const T*, const uint8_t*, doubl
 template <typename T, typename S>
 cudaError_t launch_phi_batch(const void*, const unsigned short*, int, cudaStream_t);
 template <typename T, typename S>
-cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, cudaStream_t);
+cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, cudaStream_t, bool = false);
+template <typename T, typename S>
+cudaError_t launch_mu(const Consts<T>&, const State<T, S>&, cudaStream_t);
 template <typename T, typename S>
 size_t case_desc_bytes();
 template <typename T, typename S>
@@ -87,6 +89,9 @@ struct LbmHandle {
   void* cbuf = nullptr;          // 2 x T
   double* scal = nullptr;        // [0] phi_mass_init [1] last sum [2..10] measure output
   void* meas_phi = nullptr;      // N x T scratch for lbm_measure
+  void* amp = nullptr;           // N x T per-node geometric amplification (lbm_set_amplification), or null
+  void* mu = nullptr;            // Np x T chemical potential of the step (gradient-of-mu modes only)
+  int* nsw = nullptr;            // N next-interior node indices (direct wetting only)
   // derived
   bool wetting = false;
   Consts<float> kf{};
@@ -188,20 +193,50 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   k.amp = (T)p.geo_amplification;
   // boundary-phi relaxation target (fe_ac_solver.py:165-177, 613-616)
   k.relax_on = 0;
+  k.direct = 0;
   if (k.wetting && p.boundary_relax > 0 && p.theta_eq != 90.0) {
     const double c = std::cos(th);
     const double disc = 1.0 - 4.0 * (-c / 3.0);
     double target;
     if (disc >= 0) target = 0.5 * (1.0 - std::sqrt(disc));
     else target = 0.5 * (1.0 - std::cos(M_PI - th));
-    if (std::fabs(target - 0.5) > 0.05) {
+    if (p.direct_wetting) {
+      // cubic wall energy (fe_ac_solver.py:609-612, fe_wetting.py:369-416)
+      const double a = 6.0 * p.sigma * c / p.kappa, oma = 1.0 - a;
+      k.relax_on = 1;
+      k.direct = 1;
+      k.relax_r = (T)p.boundary_relax;
+      k.cubic_on = std::fabs(a) >= 1e-10 ? 1 : 0;
+      k.cub_oma2 = (T)(oma * oma);
+      k.cub_four_a = (T)(4.0 * a);
+      k.cub_neg_oma = (T)(-oma);
+      k.cub_two_a = (T)(2.0 * a);
+    } else if (std::fabs(target - 0.5) > 0.05) {
       k.relax_on = 1;
       k.relax_target = (T)target;
       k.relax_r = (T)p.boundary_relax;
     }
   }
   for (int i = 0; i < 16; ++i) k.ww[i] = (T)ww_lut[i];
+  // interface source with grad mu (lbm/fe_ac_solver.py:457-486)
+  const double mob = cs2 * (tau_f - 0.5);
+  k.gmu_mode = p.interface_mode == LBM_IFACE_CAHN_HILLIARD ? kGmuCH : (p.mu_drive > 0.0 ? kGmuDrive : 0);
+  k.mob = (T)mob;
+  k.guo = (T)(tau_f / (tau_f - 0.5));
+  k.mu_drive_a = (T)(p.mu_drive * mob);
   return k;
+}
+
+// The constant table holds the same lattice values the kernels may also use
+// as compile-time immediates (Lat<T>).
+template <typename T>
+bool lattice_table_matches(const Consts<T>& k) {
+  for (int q = 0; q < kQ; ++q)
+    if (k.w[q] != Lat<T>::w(q) || k.wc[q] != Lat<T>::wc(q) || k.w2c[q] != Lat<T>::w2c(q) ||
+        k.inv_w[q] != Lat<T>::inv_w(q))
+      return false;
+  return k.cs2 == Lat<T>::cs2() && k.inv_cs2 == Lat<T>::inv_cs2() && k.two_cs2 == Lat<T>::two_cs2() &&
+         k.inv_two_cs2 == Lat<T>::inv_two_cs2();
 }
 
 // Compute / storage type pair of a precision: float/float, double/double,
@@ -233,6 +268,9 @@ State<T, S> make_state(const LbmHandle& h, int in_buf, int phi_in) {
   s.cls = h.cls;
   s.wn = h.wn;
   s.eps = static_cast<const T*>(h.eps);
+  s.amp = static_cast<const T*>(h.amp);
+  s.mu = static_cast<T*>(h.mu);
+  s.nsw = h.nsw;
   s.partials = h.partials;
   s.counter = h.counters;
   s.cbuf = static_cast<T*>(h.cbuf);
@@ -286,7 +324,8 @@ Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz, i
 
 void free_all(LbmHandle* h) {
   void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u,        h->phi[0], h->phi[1], h->eps,
-                  h->cls,  h->wn,   h->partials, h->counters, h->cbuf, h->scal, h->meas_phi, h->desc};
+                  h->cls,  h->wn,   h->partials, h->counters, h->cbuf, h->scal, h->meas_phi, h->desc,
+                  h->amp,  h->mu, h->nsw};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -349,7 +388,12 @@ int launch_next(LbmHandle* h, const Tiling& t, cudaStream_t st, cudaEvent_t mid)
     const unsigned char* d = static_cast<const unsigned char*>(h->desc) + par * case_desc_bytes<T, S>();
     CUDA_TRY((launch_phi_batch<T, S>(d, nullptr, phi_blocks_of(h, h->phi_per_thread), st)));
     if (mid) CUDA_TRY(cudaEventRecord(mid, st));
-    CUDA_TRY((launch_update_batch<T, S>(d, nullptr, upd_blocks_of(h), omega1_of(h), st)));
+    const bool gmu = h->mu != nullptr;
+    if (gmu) {
+      State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
+      CUDA_TRY((launch_mu<T, S>(consts_of<T>(*h), s, st)));
+    }
+    CUDA_TRY((launch_update_batch<T, S>(d, nullptr, upd_blocks_of(h), omega1_of(h), st, gmu)));
     return LBM_OK;
   }
   State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
@@ -460,6 +504,12 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   if (params->stab_mode < 0 || params->stab_mode > 2) return fail(LBM_E_ARG, "lbm_create: bad stab_mode");
   if (!(params->tau_g > 0.5) || !(params->tau_l > 0.5)) return fail(LBM_E_ARG, "lbm_create: tau_l, tau_g must exceed 0.5");
   if (!(params->xi > 0)) return fail(LBM_E_ARG, "lbm_create: xi must be positive");
+  if (params->interface_mode != LBM_IFACE_ALLEN_CAHN && params->interface_mode != LBM_IFACE_CAHN_HILLIARD)
+    return fail(LBM_E_ARG, "lbm_create: bad interface_mode");
+  if (!(params->mu_drive >= 0.0)) return fail(LBM_E_ARG, "lbm_create: mu_drive must be >= 0");
+  const bool gmu = params->interface_mode == LBM_IFACE_CAHN_HILLIARD || params->mu_drive > 0.0;
+  if (gmu && precision == LBM_F16)
+    return fail(LBM_E_UNSUPPORTED, "lbm_create: interface_mode='cahn-hilliard' and mu_drive > 0 need LBM_F32 or LBM_F64");
   LbmHandle* h = new (std::nothrow) LbmHandle();
   if (!h) return fail(LBM_E_ARG, "lbm_create: out of host memory");
   h->prm = *params;
@@ -495,6 +545,7 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   A(&h->cbuf, z.cbuf);
   A((void**)&h->scal, z.scal);
   A(&h->meas_phi, z.meas_phi);
+  if (gmu) A(&h->mu, z.phi);
   if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(h->phi[0], 0, Np * T);
   if (e == cudaSuccess) e = cudaMemset(h->phi[1], 0, Np * T);
@@ -524,6 +575,10 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
   const int64_t N = h->N;
   CUDA_TRY(cudaMemcpy(h->cls, h->geo.cls.data(), N, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(h->wn, h->geo.wall_normal.data(), 3 * N * sizeof(float), cudaMemcpyHostToDevice));
+  if (h->prm.direct_wetting) {
+    if (!h->nsw) CUDA_TRY(cudaMalloc(&h->nsw, N * sizeof(int)));
+    CUDA_TRY(cudaMemcpy(h->nsw, h->geo.nsw.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  }
   if (h->prec != LBM_F64) {
     std::vector<float> eps(N, 0.0f);
     if (!h->geo.fraction.empty())
@@ -538,7 +593,40 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
   near_wall_weights(lut);
   h->kf = make_consts<float>(*h, lut);
   h->kd = make_consts<double>(*h, lut);
+  if (!lattice_table_matches(h->kf) || !lattice_table_matches(h->kd))
+    return fail(LBM_E_ARG, "lbm_set_geometry: internal error: lattice constant table differs from the kernels' immediates");
   h->geometry_set = true;
+  h->desc_ok = false;
+  return LBM_OK;
+}
+
+int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype) {
+  if (!h) return fail(LBM_E_ARG, "lbm_set_amplification: null handle");
+  if (!alpha) {
+    if (alpha_dtype != LBM_DT_NONE) return fail(LBM_E_ARG, "lbm_set_amplification: alpha and alpha_dtype disagree");
+    if (h->amp) {
+      // steps already queued may still read the field
+      CUDA_TRY(cudaDeviceSynchronize());
+      CUDA_TRY(cudaFree(h->amp));
+      h->amp = nullptr;
+    }
+    h->desc_ok = false;
+    return LBM_OK;
+  }
+  if (alpha_dtype != LBM_DT_F32 && alpha_dtype != LBM_DT_F64)
+    return fail(LBM_E_ARG, "lbm_set_amplification: alpha_dtype must be LBM_DT_F32 or LBM_DT_F64");
+  const int64_t N = h->N;
+  // the reference casts the field to the compute type (fe_wetting.py:505)
+  std::vector<unsigned char> buf(N * h->tsize);
+  for (int64_t n = 0; n < N; ++n) {
+    const double a = alpha_dtype == LBM_DT_F32 ? (double)static_cast<const float*>(alpha)[n]
+                                               : static_cast<const double*>(alpha)[n];
+    if (h->prec == LBM_F64) reinterpret_cast<double*>(buf.data())[n] = a;
+    else reinterpret_cast<float*>(buf.data())[n] = (float)a;
+  }
+  if (!h->amp) CUDA_TRY(cudaMalloc(&h->amp, N * h->tsize));
+  else CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(h->amp, buf.data(), N * h->tsize, cudaMemcpyHostToDevice));
   h->desc_ok = false;
   return LBM_OK;
 }
@@ -631,6 +719,8 @@ int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz) {
   if (tx == 1 || ty == 1 || tz == 1 || tx < 0 || ty < 0 || tz < 0 || tx > 64 || ty > 64 || tz > 256)
     return fail(LBM_E_ARG, "lbm_set_tile: tile extents must be in [2, 64] x [2, 64] x [2, 256] (0 = automatic)");
   Tiling t = make_tiling(h->nx, h->ny, h->nz, tx, ty, tz, h->prec);
+  if (t.tx != 0 && h->mu)
+    return fail(LBM_E_UNSUPPORTED, "lbm_set_tile: the gradient-of-mu modes run the two-kernel step only");
   if (tiling_smem(t, h->prec) > 220 * 1024) return fail(LBM_E_ARG, "lbm_set_tile: tile too large for shared memory");
   h->tiling = t;
   return LBM_OK;
@@ -653,7 +743,9 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
   // x-y cross-sections of 4..16 nodes, shared memory within a third of an SM
   std::vector<Tiling> cands;
   cands.push_back(make_tiling(h->nx, h->ny, h->nz, 0, 0, 0, h->prec));  // two-kernel step
+  // (the gradient-of-mu modes have no fused-kernel form)
   for (int zt : {24, 32, 48, 64}) {
+    if (h->mu) break;
     const int ntz = (int)((h->nz + zt - 1) / zt);
     const int tz = (int)((h->nz + ntz - 1) / ntz);
     for (int sx : {4, 5, 6, 8, 10, 12}) for (int sy : {4, 5, 6, 8, 10, 12}) {
@@ -888,6 +980,133 @@ int lbm_measure(LbmHandle* h, double* out9, void* stream) {
   return LBM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Checkpoints: the complete time-stepping state of a handle as one host blob
+// ---------------------------------------------------------------------------
+namespace {
+constexpr uint32_t kStateMagic = 0x534d424cu;  // "LBMS"
+constexpr uint32_t kStateVersion = 1;
+
+struct StateHeader {
+  uint32_t magic, version;
+  int64_t nx, ny, nz;
+  int32_t prec, cur, pc, c_last;
+  int32_t raw, first, last_raw_in, obs_init;
+  int64_t steps;
+  uint64_t geometry_hash;  // FNV-1a of the node-class table (the geometry the state belongs to)
+  uint32_t status;
+  uint32_t reserved;
+};
+
+uint64_t fnv1a(const uint8_t* p, size_t n) {
+  uint64_t x = 1469598103934665603ull;
+  for (size_t i = 0; i < n; ++i) x = (x ^ p[i]) * 1099511628211ull;
+  return x;
+}
+
+// Device arrays of a checkpoint, in blob order: f and g of the current
+// buffer, g of the other buffer, u, both phi buffers, the two
+// mass-correction factors, the scalars.
+struct StatePart {
+  void* dev;
+  size_t bytes;
+};
+std::vector<StatePart> state_parts(LbmHandle* h) {
+  const size_t pop = (size_t)Q * h->Np * h->psize;
+  // g of the last step's input buffer: the pressure read-out after a step sums it
+  return {{h->f[h->cur], pop},
+          {h->g[h->cur], pop},
+          {h->g[h->cur ^ 1], pop},
+          {h->u, 3 * (size_t)h->Np * h->tsize},
+          {h->phi[0], (size_t)h->Np * h->tsize},
+          {h->phi[1], (size_t)h->Np * h->tsize},
+          {h->cbuf, 2 * h->tsize},
+          {h->scal, 2 * sizeof(double)}};
+}
+size_t state_bytes(LbmHandle* h) {
+  size_t b = sizeof(StateHeader);
+  for (const StatePart& p : state_parts(h)) b += p.bytes;
+  return b;
+}
+}  // namespace
+
+int lbm_state_bytes(LbmHandle* h, int64_t* bytes) {
+  if (!h || !bytes) return fail(LBM_E_ARG, "lbm_state_bytes: null argument");
+  *bytes = (int64_t)state_bytes(h);
+  return LBM_OK;
+}
+
+int lbm_save_state(LbmHandle* h, void* host, int64_t bytes, void* stream) {
+  if (!h || !host) return fail(LBM_E_ARG, "lbm_save_state: null argument");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_save_state: call lbm_init_fields first");
+  if (bytes != (int64_t)state_bytes(h)) return fail(LBM_E_ARG, "lbm_save_state: buffer size is not lbm_state_bytes");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  StateHeader hd;
+  std::memset(&hd, 0, sizeof(hd));
+  hd.magic = kStateMagic;
+  hd.version = kStateVersion;
+  hd.nx = h->nx;
+  hd.ny = h->ny;
+  hd.nz = h->nz;
+  hd.prec = h->prec;
+  hd.cur = h->cur;
+  hd.pc = h->pc;
+  hd.c_last = h->c_last;
+  hd.raw = h->raw;
+  hd.first = h->first;
+  hd.last_raw_in = h->last_raw_in;
+  hd.obs_init = h->obs_init;
+  hd.steps = h->steps;
+  hd.geometry_hash = fnv1a(h->geo.cls.data(), h->geo.cls.size());
+  CUDA_TRY(cudaMemcpyAsync(&hd.status, h->counters + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  char* out = static_cast<char*>(host) + sizeof(StateHeader);
+  for (const StatePart& p : state_parts(h)) {
+    CUDA_TRY(cudaMemcpyAsync(out, p.dev, p.bytes, cudaMemcpyDeviceToHost, st));
+    out += p.bytes;
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  std::memcpy(host, &hd, sizeof(hd));
+  return LBM_OK;
+}
+
+int lbm_load_state(LbmHandle* h, const void* host, int64_t bytes, void* stream) {
+  if (!h || !host) return fail(LBM_E_ARG, "lbm_load_state: null argument");
+  if (!h->geometry_set) return fail(LBM_E_STATE, "lbm_load_state: call lbm_set_geometry first");
+  if (bytes < (int64_t)sizeof(StateHeader)) return fail(LBM_E_ARG, "lbm_load_state: buffer too small");
+  StateHeader hd;
+  std::memcpy(&hd, host, sizeof(hd));
+  if (hd.magic != kStateMagic || hd.version != kStateVersion)
+    return fail(LBM_E_ARG, "lbm_load_state: not a state written by lbm_save_state (bad magic or version)");
+  if (hd.nx != h->nx || hd.ny != h->ny || hd.nz != h->nz || hd.prec != h->prec)
+    return fail(LBM_E_ARG, "lbm_load_state: the state belongs to a different grid or precision");
+  if (hd.geometry_hash != fnv1a(h->geo.cls.data(), h->geo.cls.size()))
+    return fail(LBM_E_ARG, "lbm_load_state: the state belongs to a different geometry");
+  if (bytes != (int64_t)state_bytes(h)) return fail(LBM_E_ARG, "lbm_load_state: buffer size is not lbm_state_bytes");
+  if ((hd.cur & ~1) || (hd.pc & ~1) || (hd.c_last & ~1) || hd.steps < 0)
+    return fail(LBM_E_ARG, "lbm_load_state: corrupt header");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // queued steps may still read the buffers about to be overwritten
+  CUDA_TRY(cudaStreamSynchronize(st));
+  h->cur = hd.cur;
+  h->pc = hd.pc;
+  h->c_last = hd.c_last;
+  const char* in = static_cast<const char*>(host) + sizeof(StateHeader);
+  for (const StatePart& p : state_parts(h)) {
+    CUDA_TRY(cudaMemcpyAsync(p.dev, in, p.bytes, cudaMemcpyHostToDevice, st));
+    in += p.bytes;
+  }
+  CUDA_TRY(cudaMemcpyAsync(h->counters + 2, &hd.status, sizeof(unsigned), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  h->raw = hd.raw != 0;
+  h->first = hd.first != 0;
+  h->last_raw_in = hd.last_raw_in != 0;
+  h->obs_init = hd.obs_init != 0;
+  h->steps = hd.steps;
+  h->initialized = true;
+  h->desc_ok = false;
+  return LBM_OK;
+}
+
 int lbm_status(LbmHandle* h, uint32_t* flags) {
   if (!h || !flags) return fail(LBM_E_ARG, "lbm_status: null argument");
   unsigned v = 0;
@@ -1069,6 +1288,9 @@ int lbm_batch_create(LbmHandle* const* handles, int n, LbmBatch** out) {
                              "their geometry set");
     for (int j = 0; j < i; ++j)
       if (handles[j] == h) return fail(LBM_E_ARG, "lbm_batch_create: a handle appears twice");
+    if (h->mu)
+      return fail(LBM_E_UNSUPPORTED, "lbm_batch_create: the gradient-of-mu modes (cahn-hilliard, mu_drive) step "
+                                     "one grid at a time");
   }
   LbmBatch* b = new (std::nothrow) LbmBatch();
   if (!b) return fail(LBM_E_ARG, "lbm_batch_create: out of host memory");

@@ -32,6 +32,26 @@ __host__ __device__ constexpr int opp(int q) {
 }
 __host__ __device__ constexpr int ecomp(int q, int d) { return d == 0 ? ex(q) : (d == 1 ? ey(q) : ez(q)); }
 
+// D3Q19 lattice constants as compile-time values in the compute type T: the
+// float32 weights of the reference (lbm/lattice.py:82-88, float32 even in
+// float64 runs) widened to T, c_s^2 = 1/3 rounded to T, and the products the
+// step uses.  Each is the same single rounding the host applies when it fills
+// Consts (checked when a grid's constants are built), so kernels may use either;
+// as immediates they cost no loads.
+template <typename T>
+struct Lat {
+  __host__ __device__ static constexpr T w(int q) {
+    return q == 0 ? T(float(1.0 / 3.0)) : (q <= 6 ? T(float(1.0 / 18.0)) : T(float(1.0 / 36.0)));
+  }
+  __host__ __device__ static constexpr T cs2() { return T(1.0 / 3.0); }
+  __host__ __device__ static constexpr T inv_cs2() { return T(1) / cs2(); }
+  __host__ __device__ static constexpr T two_cs2() { return T(2.0 * (1.0 / 3.0)); }
+  __host__ __device__ static constexpr T inv_two_cs2() { return T(1) / two_cs2(); }
+  __host__ __device__ static constexpr T wc(int q) { return w(q) / cs2(); }       // w_q / cs2
+  __host__ __device__ static constexpr T w2c(int q) { return T(2) * wc(q); }      // 2 w_q / cs2
+  __host__ __device__ static constexpr T inv_w(int q) { return T(1) / w(q); }     // 1 / w_q
+};
+
 // Node class byte.
 constexpr uint8_t kSolid = 1;     // solid node (bounce-back)
 constexpr uint8_t kBoundary = 2;  // fluid node with a solid D3Q19 neighbour (wetting)
@@ -143,8 +163,18 @@ struct Consts {
   T mu_wall_add;         // mu_wall * mu_wall_scale (linear)
   T cos_t, sin_t, amp;
   T relax_r, relax_target;
+  // cubic-wall-energy boundary phi (direct wetting, fe_wetting.py:369-416):
+  // target root of a phi_b^2 + (1 - a) phi_b - phi_nsw = 0, a = 6 sigma cos(theta) / kappa
+  int direct, cubic_on;
+  T cub_oma2, cub_four_a, cub_neg_oma, cub_two_a;  // (1 - a)^2, 4 a, -(1 - a), 2 a
   T ww[16];              // near-wall weight by code (float32 values)
+  // chemical-potential gradient terms of the interface source
+  // (lbm/fe_ac_solver.py:457-486): 0 none, kGmuCH Cahn-Hilliard, kGmuDrive mu_drive
+  int gmu_mode;
+  T mob, guo, mu_drive_a;  // mobility cs2 (tau_f - 1/2), tau_f / (tau_f - 1/2), mu_drive * mobility
 };
+constexpr int kGmuCH = 1;
+constexpr int kGmuDrive = 2;
 
 // Device state of one grid.  T is the compute type, S the population
 // storage type (T itself, or half for the deviation-storage form).
@@ -160,6 +190,9 @@ struct State {
   const uint8_t* cls;
   const float* wn;  // wall normal [3][N] (non-zero at boundary nodes only)
   const T* eps;     // solid fraction (read at partial nodes only)
+  const T* amp;     // per-node geometric amplification (read at boundary nodes only; null: the scalar k.amp)
+  T* mu;            // chemical potential of this step [N] (k_mu; the gradient-of-mu modes only)
+  const int* nsw;   // next-interior fluid node of a boundary node or -1 [N] (direct wetting only)
   double* partials; // one per block
   unsigned* counter;
   T* cbuf;          // mass-correction factor of the last two steps

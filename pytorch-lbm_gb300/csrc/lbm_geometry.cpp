@@ -8,6 +8,7 @@
 // numpy's float32/float64 operation sequence exactly.
 #include "lbm_geometry.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -199,6 +200,27 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
       }
       g.top[n] = top ? 1 : 0;
     }
+    // next-interior node of each boundary node for the cubic-wall-energy
+    // boundary phi: one step along the wall normal rounded half to even,
+    // clamped to the grid (not periodic); kept only where that node is fluid
+    // (fe_wetting.py:313-367)
+    g.nsw.assign(N, -1);
+    for (int64_t ix = 0; ix < nx; ++ix)
+      for (int64_t iy = 0; iy < ny; ++iy)
+        for (int64_t iz = 0; iz < nz; ++iz) {
+          const int64_t n = idx(ix, iy, iz, ny, nz);
+          if (!g.boundary[n]) continue;
+          const int64_t c[3] = {ix, iy, iz}, ext[3] = {nx, ny, nz};
+          int64_t t[3];
+          for (int d = 0; d < 3; ++d) {
+            const int64_t sh = (int64_t)std::nearbyint(g.wall_normal[d * N + n]);
+            t[d] = std::min<int64_t>(std::max<int64_t>(c[d] + sh, 0), ext[d] - 1);
+          }
+          const int64_t m = idx(t[0], t[1], t[2], ny, nz);
+          if (!g.solid[m]) g.nsw[n] = (int32_t)m;
+        }
+  } else {
+    g.nsw.assign(N, -1);
   }
   // node-class byte
   g.cls.assign(N, 0);

@@ -11,6 +11,7 @@ struct Geometry {
   std::vector<float> wall_weight;  // [N]
   std::vector<int> dist;           // near-wall distance (100 = not reached)
   std::vector<double> fraction;    // solid fraction as given (empty if none)
+  std::vector<int32_t> nsw;        // next-interior fluid node of a boundary node, else -1
   int64_t n_boundary = 0;
 };
 

@@ -124,16 +124,16 @@ template <>
 struct PopIO<float, __half> {
   static constexpr bool kDev = true;
   __device__ __forceinline__ static float ld_f(__half raw, int q, float ref, const Consts<float>& k) {
-    return k.w[q] * (__half2float(raw) + ref);
+    return Lat<float>::w(q) * (__half2float(raw) + ref);
   }
   __device__ __forceinline__ static __half st_f(float v, int q, float ref, const Consts<float>& k) {
-    return __float2half_rn(v * k.inv_w[q] - ref);
+    return __float2half_rn(v * Lat<float>::inv_w(q) - ref);
   }
   __device__ __forceinline__ static float ld_g(__half raw, int q, const Consts<float>& k) {
-    return k.w[q] * __half2float(raw);
+    return Lat<float>::w(q) * __half2float(raw);
   }
   __device__ __forceinline__ static __half st_g(float v, int q, const Consts<float>& k) {
-    return __float2half_rn(v * k.inv_w[q]);
+    return __float2half_rn(v * Lat<float>::inv_w(q));
   }
 };
 
@@ -266,14 +266,29 @@ __device__ __forceinline__ T seqsum(const T (&v)[Q]) {
   return s;
 }
 
-// Boundary-phi relaxation target of a top-surface boundary node from the
-// previous step's phi and mass correction (lbm/fe_ac_solver.py:594-624);
-// negative when the node is not active.
+// Boundary-phi relaxation target of top-surface boundary node n from the
+// previous step's phi (phi_prev = phi_arr[n]) and mass correction
+// (lbm/fe_ac_solver.py:594-624); negative when the node is not active.  With
+// direct wetting the target is the cubic-wall-energy boundary phi from the
+// corrected phi of the node's next-interior node (fe_wetting.py:369-416), or
+// the node's own phi where that does not apply.
 template <typename T>
-__device__ __forceinline__ T relax_target(const Consts<T>& k, T phi_prev, T corr) {
+__device__ __forceinline__ T relax_target(const Consts<T>& k, const T* __restrict__ phi_arr,
+                                          const int* __restrict__ nsw, int n, T phi_prev, T corr) {
   const T pb = clamp01(phi_prev * corr);
-  if (pb > T(0.15) && pb < T(0.85)) return clamp01(pb + k.relax_r * (k.relax_target - pb));
-  return T(-1);
+  if (!(pb > T(0.15) && pb < T(0.85))) return T(-1);
+  T target = k.relax_target;
+  if (k.direct) {
+    target = pb;
+    const int m = nsw[n];
+    if (k.cubic_on && m >= 0 && pb > T(0.01) && pb < T(0.99)) {
+      const T pn = clamp01(phi_arr[m] * corr);
+      T disc = k.cub_oma2 + k.cub_four_a * pn;
+      disc = disc < T(0) ? T(0) : disc;
+      target = clamp01((k.cub_neg_oma + sqrt(disc)) / k.cub_two_a);
+    }
+  }
+  return clamp01(pb + k.relax_r * (target - pb));
 }
 
 // Relaxation scale of lbm/fe_ac_solver.py:626-629.
@@ -291,7 +306,7 @@ __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const Sta
   const T corr = RAW ? T(1) : s.cbuf[s.c_prev];
   fetch_pop<T, S, RAW, !RAW, true, USE_POL>(v, k, s.fin, s.phi_in, n, N, nb, c, eps, corr, pol);
   if (!RAW && k.relax_on && (c & kTop)) {
-    const T r = relax_target(k, ldg(s.phi_in + n), corr);
+    const T r = relax_target(k, s.phi_in, s.nsw, n, ldg(s.phi_in + n), corr);
     if (r >= T(0)) {
       const T sc = relax_scale(r, seqsum(v));
 #pragma unroll
@@ -299,6 +314,23 @@ __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const Sta
     }
   }
 }
+
+// Lattice constants as the step kernels read them: compile-time immediates
+// (IMM) or the grid's constant table.  Both hold the same values (the table is
+// checked against the immediates when it is built); which is faster depends
+// on the kernel's register allocation (measured on the 150x150x107 case:
+// immediates for the half-storage form, 0.1829 -> 0.1797 ms per step; the
+// table for float storage, 0.1746 -> 0.1698).
+template <typename T, bool IMM>
+struct LatK {
+  const Consts<T>& k;
+  __device__ __forceinline__ T w(int q) const { return IMM ? Lat<T>::w(q) : k.w[q]; }
+  __device__ __forceinline__ T wc(int q) const { return IMM ? Lat<T>::wc(q) : k.wc[q]; }
+  __device__ __forceinline__ T w2c(int q) const { return IMM ? Lat<T>::w2c(q) : k.w2c[q]; }
+  __device__ __forceinline__ T cs2() const { return IMM ? Lat<T>::cs2() : k.cs2; }
+  __device__ __forceinline__ T inv_cs2() const { return IMM ? Lat<T>::inv_cs2() : k.inv_cs2; }
+  __device__ __forceinline__ T inv_two_cs2() const { return IMM ? Lat<T>::inv_two_cs2() : k.inv_two_cs2; }
+};
 
 // ---------------------------------------------------------------------------
 // Isotropic gradient / laplacian with the ghost-node wetting correction
@@ -310,9 +342,10 @@ __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const Sta
 // mirror partners summed first so that a mirror-symmetric phi still gives
 // an exactly zero component (the sharpening normal grad / |grad| depends on
 // it where the gradient vanishes).
-template <typename T, bool FUSED, typename St, typename SolidFn, bool PAIR = false>
+template <typename T, bool FUSED, typename St, typename SolidFn, bool PAIR = false, bool IMM = false>
 __device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n, uint8_t c, T phi,
                                          T (&ps)[Q], SolidFn nsolid, T& gx, T& gy, T& gz, T& lap) {
+  const LatK<T, IMM> L{k};
   if (k.wetting && (c & kBoundary)) {
     const size_t N = (size_t)k.N;
     const float n0 = s.wn[n], n1 = s.wn[N + n], n2 = s.wn[2 * N + n];
@@ -333,7 +366,7 @@ __device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n,
   }
   gx = gy = gz = lap = T(0);
   if constexpr (PAIR) {
-    auto t = [&](int q) { return mul_rn(k.wc[q], ps[q] - ps[opp(q)]); };
+    auto t = [&](int q) { return mul_rn(L.wc(q), ps[q] - ps[opp(q)]); };
     const T t1 = t(1), t3 = t(3), t5 = t(5), t7 = t(7), t8 = t(8), t11 = t(11), t12 = t(12), t15 = t(15),
             t16 = t(16);
     gx = add_rn(add_rn(t1, t7 - t8), t11 - t12);  // e_x: q 1, 7, -8, 11, -12 (and their opposites)
@@ -343,14 +376,14 @@ __device__ __forceinline__ void grad_lap(const Consts<T>& k, const St& s, int n,
 #pragma unroll
   for (int q = 1; q < Q; ++q) {
     if (!PAIR) {
-      if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
-      if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
-      if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? k.wc[q] : -k.wc[q], ps[q]));
+      if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? L.wc(q) : -L.wc(q), ps[q]));
+      if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? L.wc(q) : -L.wc(q), ps[q]));
+      if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? L.wc(q) : -L.wc(q), ps[q]));
     }
     if (FUSED) {
-      lap = fma_(k.w2c[q], ps[q] - phi, lap);
+      lap = fma_(L.w2c(q), ps[q] - phi, lap);
     } else {
-      lap = lap + (T(2) * k.w[q]) * (ps[q] - phi) / k.cs2;
+      lap = lap + (T(2) * L.w(q)) * (ps[q] - phi) / L.cs2();
     }
   }
 }
@@ -364,6 +397,40 @@ __device__ __forceinline__ T chem_pot(const Consts<T>& k, uint8_t c, T phi, T la
     else mu = mu + k.phi_c * phi * (T(1) - phi);
   }
   return mu;
+}
+
+// Isotropic gradient of the chemical potential (the reference's unfused
+// _lattice_gradient(mu_phi), lbm/fe_ac_solver.py:267-280), with the ghost
+// correction of fe_wetting.py:418-446 applied to mu itself at a boundary
+// node's solid neighbours: per direction q in order, per axis with
+// e_q != 0, grad += ((w_q e_q) mu(x + e_q)) / cs2.
+template <typename T, typename St, typename MuAt, typename SolidFn>
+__device__ __forceinline__ void grad_mu(const Consts<T>& k, const St& s, int n, uint8_t c, T mu, MuAt mu_at,
+                                        SolidFn nsolid, T& gx, T& gy, T& gz) {
+  const bool ghost = k.wetting && (c & kBoundary);
+  float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+  if (ghost) {
+    const size_t N = (size_t)k.N;
+    n0 = s.wn[n];
+    n1 = s.wn[N + n];
+    n2 = s.wn[2 * N + n];
+  }
+  gx = gy = gz = T(0);
+#pragma unroll
+  for (int q = 1; q < Q; ++q) {
+    T v = mu_at(q);
+    if (ghost && nsolid(q)) {
+      float nde = 0.0f;
+      nde = __fadd_rn(nde, __fmul_rn(n0, (float)ex(q)));
+      nde = __fadd_rn(nde, __fmul_rn(n1, (float)ey(q)));
+      nde = __fadd_rn(nde, __fmul_rn(n2, (float)ez(q)));
+      v = k.linear ? mu - (T)__fmul_rn(nde, k.h_over_kappa_f) : mu + (T)__fmul_rn(nde, k.pcok_f) * mu * (T(1) - mu);
+    }
+    const T w = Lat<T>::w(q);
+    if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? w : -w, v) / Lat<T>::cs2());
+    if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? w : -w, v) / Lat<T>::cs2());
+    if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? w : -w, v) / Lat<T>::cs2());
+  }
 }
 
 // e_q . (a0, a1, a2) with the reference's exact two-term sums.
@@ -418,12 +485,14 @@ __device__ __forceinline__ void stage_node(const Consts<T>& k, const State<T, T>
 
 // STAGED: g, u and the previous phi come from the node's cp.async staging
 // slot `st` (word j at st[j * kBlock]); otherwise they are loaded here.
-template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool STAGED, bool STORE_PHI, typename PhiAt,
-          typename SolidAt>
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool STAGED, bool STORE_PHI, bool GMU,
+          typename PhiAt, typename SolidAt, typename RefAt>
 __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S>& s, int n, const Nbr& nb,
-                                            uint8_t c, T phi, PhiAt phi_at, SolidAt solid_at, const Pol& pol,
-                                            const T* st) {
+                                            uint8_t c, T phi, PhiAt phi_at, SolidAt solid_at, RefAt ref_at,
+                                            const Pol& pol, const T* st) {
   using IO = PopIO<T, S>;
+  constexpr bool IMM = IO::kDev;
+  const LatK<T, IMM> L{k};
   const size_t N = (size_t)k.N;
   const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
 
@@ -432,7 +501,7 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
 #pragma unroll
   for (int q = 1; q < Q; ++q) ps[q] = phi_at(q);
   T gx, gy, gz, lap;
-  grad_lap<T, true, State<T, S>, SolidAt, true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
+  grad_lap<T, true, State<T, S>, SolidAt, true, IMM>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
 
   // then g (pulled), u and phi of the last step.  Loading them after the
   // stencil keeps the 18 stencil values and the 19 populations from being
@@ -471,7 +540,9 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
 
   const T rho = fma_(phi, k.rho_l, (T(1) - phi) * k.rho_g);
   const T rho_eff = rho < k.rho_floor ? k.rho_floor : rho;
-  const T mu = chem_pot(k, c, phi, lap);
+  // with a chemical-potential gradient term, mu of every node comes from k_mu
+  // (the same arithmetic), so that the node's own mu and its neighbours' agree
+  const T mu = GMU ? ld_pol(s.mu + n, pol.keep) : chem_pot(k, c, phi, lap);
 
   // geometric contact-angle gradient correction (fe_wetting.py:448-539).  The
   // wall normal is zero away from boundary nodes, where the correction is the
@@ -483,7 +554,11 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     T tm = sqrt(add_rn(add_rn(mul_rn(tx, tx), mul_rn(ty, ty)), mul_rn(tz, tz)));
     tm = tm < T(1e-10) ? T(1e-10) : tm;
     T gd = mul_rn(-tm, k.cos_t) / k.sin_t;
-    if (k.amp_active) {
+    if (s.amp) {
+      // per-node amplification field: active where alpha > 1 (fe_wetting.py:503-512)
+      const T a = s.amp[n];
+      if (a > T(1)) gd = add_rn(gn, mul_rn(gd - gn, a));
+    } else if (k.amp_active) {
       const T delta = gd - gn;
       gd = add_rn(gn, mul_rn(delta, k.amp));
     }
@@ -515,7 +590,7 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   for (int i = 0; i < 9; ++i) P = P + sp[i];
   T sxx, syy, szz, sxy, sxz, syz;
   {
-    const T pc = P * k.cs2;
+    const T pc = P * L.cs2();
     sxx = fma_(-uo0, uo0, (sp[0] + (sp[3] + sp[4]) + (sp[5] + sp[6])) - pc);
     syy = fma_(-uo1, uo1, (sp[1] + (sp[3] + sp[4]) + (sp[7] + sp[8])) - pc);
     szz = fma_(-uo2, uo2, (sp[2] + (sp[5] + sp[6]) + (sp[7] + sp[8])) - pc);
@@ -527,7 +602,7 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   // 5. forces (Fakhari 2017, :416-439)
   T F0 = mu * gx, F1 = mu * gy, F2 = mu * gz;
   if (k.stab_mode <= 1) {
-    const T fp = ((-P) * k.drho) * k.cs2;
+    const T fp = ((-P) * k.drho) * L.cs2();
     F0 = fma_(fp, gx, F0);
     F1 = fma_(fp, gy, F1);
     F2 = fma_(fp, gz, F2);
@@ -552,7 +627,7 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     u2 = fma_(F2, hr, dp[2] + (dp[5] + dp[6]) + (dp[7] + dp[8]));
     if (c & kSolid) u0 = u1 = u2 = T(0);
   }
-  const T b = fma_(u2, u2, fma_(u1, u1, u0 * u0)) * k.inv_two_cs2;
+  const T b = fma_(u2, u2, fma_(u1, u1, u0 * u0)) * L.inv_two_cs2();
 
   // 7. Allen-Cahn source (:450-494)
   T S0, S1, S2;
@@ -566,11 +641,28 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     T gm = sqrt(fma_(gz, gz, fma_(gy, gy, gx * gx)));
     gm = gm < T(1e-10) ? T(1e-10) : gm;
     const T lam = ((T(4) * phi) * (T(1) - phi)) * k.inv_W;
-    T cl = k.cs2 * lam * k.ac_scale * rcp(gm);
+    T cl = L.cs2() * lam * k.ac_scale * rcp(gm);
     if (k.wetting) cl = cl * (T(1) - k.sharpen_reduce * k.ww[c >> kWwShift]);
-    S0 = fma_(cl, gx, d0);
-    S1 = fma_(cl, gy, d1);
-    S2 = fma_(cl, gz, d2);
+    if constexpr (GMU) {
+      T mx, my, mz;
+      grad_mu(k, s, n, c, mu, [&](int q) { return ld_pol(s.mu + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); },
+              solid_at, mx, my, mz);
+      if (k.gmu_mode == kGmuCH) {
+        // Cahn-Hilliard: d(phi u) + M (grad mu - grad phi) tau_f / (tau_f - 1/2)  (:457-461)
+        S0 = d0 + (k.mob * (mx - gx)) * k.guo;
+        S1 = d1 + (k.mob * (my - gy)) * k.guo;
+        S2 = d2 + (k.mob * (mz - gz)) * k.guo;
+      } else {
+        // Allen-Cahn with the mu drive: sharpening + d(phi u) + mu_drive M grad mu  (:484-486)
+        S0 = fma_(cl, gx, d0) + k.mu_drive_a * mx;
+        S1 = fma_(cl, gy, d1) + k.mu_drive_a * my;
+        S2 = fma_(cl, gz, d2) + k.mu_drive_a * mz;
+      }
+    } else {
+      S0 = fma_(cl, gx, d0);
+      S1 = fma_(cl, gy, d1);
+      S2 = fma_(cl, gz, d2);
+    }
   }
 
   // 8. both BGK collisions (:496-530) one opposite pair (q, opp q) at a time.
@@ -588,27 +680,27 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     om = rcp(T(0.5) + eta / rden);
   }
   const T omo = T(1) - om;
-  const T nsd = (T(1) - om * T(0.5)) * rcp(rho_eff * k.cs2);
+  const T nsd = (T(1) - om * T(0.5)) * rcp(rho_eff * L.cs2());
   const T Pb = P - b;
   const T omb = T(1) - b;
   const T pf = OMEGA1 ? phi : k.omega_f * phi;  // omega_f phi
-  const T u3x = u0 * k.inv_cs2, u3y = u1 * k.inv_cs2, u3z = u2 * k.inv_cs2;
+  const T u3x = u0 * L.inv_cs2(), u3y = u1 * L.inv_cs2(), u3z = u2 * L.inv_cs2();
   T f[Q];
   if (!OMEGA1) fetch_f<T, S, RAW, true>(f, k, s, n, N, nb, c, eps, pol.same);
   auto store_g = [&](int q, T v) { st_pol(s.gout + (q * Nu + nu), IO::st_g(v, q, k), pol.once); };
   auto store_f = [&](int q, T v) {
-    st_pol(s.fout + (q * Nu + nu), IO::st_f(v, q, IO::kDev ? phi_at(q) : T(0), k), pol.once);
+    st_pol(s.fout + (q * Nu + nu), IO::st_f(v, q, IO::kDev ? ref_at(q) : T(0), k), pol.once);
   };
   {
-    const T ow = om * k.w[0];
+    const T ow = om * L.w(0);
     store_g(0, fma_(omo, g[0], ow * Pb));
-    const T pw = pf * k.w[0];
+    const T pw = pf * L.w(0);
     const T f0 = pw * omb;
     store_f(0, OMEGA1 ? f0 : fma_(T(1) - k.omega_f, f[0], f0));
   }
   // per weight class (axis pairs i < 3, diagonal pairs i >= 3): omega w,
   // omega w / 2, omega w (P - b), nsd w; omega_f phi w, its half, omega_f phi w (1 - b)
-  const T wa = k.w[1], wd = k.w[7];
+  const T wa = L.w(1), wd = L.w(7);
   const T owa = om * wa, owd = om * wd;
   const T howa = T(0.5) * owa, howd = T(0.5) * owd;
   const T obpa = owa * Pb, obpd = owd * Pb;
@@ -888,9 +980,10 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
       const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
       // phi of this step at x + e_q (also the deviation reference, in the half
       // form, of the next step's reader of slot (x, q))
-      update_node<T, S, RAW, FIRST, OMEGA1, STAGED, true>(
+      update_node<T, S, RAW, FIRST, OMEGA1, STAGED, true, false>(
           k, s, n, nb, scls[h], sphi[h], [&](int q) { return sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)]; },
-          [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; }, pol,
+          [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; },
+          [&](int q) { return sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)]; }, pol,
           stage + (j & 1) * kStage * kBlock + threadIdx.x);
     }
   }
@@ -963,12 +1056,12 @@ __global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
   phi_finish(s, part, blockIdx.x, gridDim.x);
 }
 
-template <typename T, typename S>
+template <typename T, typename S, bool GMU = false>
 struct UpdateOccupancy {
-  static constexpr int blocks = sizeof(T) == 8 ? 1 : (sizeof(S) == 2 ? 3 : 4);
+  static constexpr int blocks = sizeof(T) == 8 ? 1 : ((sizeof(S) == 2 || GMU) ? 3 : 4);
 };
 
-template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool GMU>
 __device__ __forceinline__ void update_one(const Consts<T>& k, const State<T, S>& s, int n, const Pol& pol) {
   int ix, iy, iz;
   decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
@@ -976,9 +1069,10 @@ __device__ __forceinline__ void update_one(const Consts<T>& k, const State<T, S>
   const T* __restrict__ pc = s.phi_out;  // phi of this step (k_phi)
   const uint8_t c = s.cls[n];
   const T phi = ld_pol(pc + n, pol.keep);
-  update_node<T, S, RAW, FIRST, OMEGA1, false, false>(
+  update_node<T, S, RAW, FIRST, OMEGA1, false, false, GMU>(
       k, s, n, nb, c, phi, [&](int q) { return ld_pol(pc + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); },
-      [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; }, pol, (const T*)nullptr);
+      [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; },
+      [&](int q) { return ld_pol(pc + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); }, pol, (const T*)nullptr);
 }
 
 // One thread per node, linear order.  (Measured slower on the 150x150x107
@@ -986,10 +1080,33 @@ __device__ __forceinline__ void update_one(const Consts<T>& k, const State<T, S>
 // g, u and previous phi in shared memory with cp.async or with bulk copies
 // per chunk of nodes -- the copies, the smaller L1 and the block-wide waits
 // cost more than the latency they hide.)
-template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1>
-__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_update(Consts<T> k, State<T, S> s) {
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool GMU = false>
+__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S, GMU>::blocks) k_update(Consts<T> k, State<T, S> s) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
-  if (n < k.N) update_one<T, S, RAW, FIRST, OMEGA1>(k, s, n, Pol::make());
+  if (n < k.N) update_one<T, S, RAW, FIRST, OMEGA1, GMU>(k, s, n, Pol::make());
+}
+
+// Chemical potential of every node of this step (phi from the phi kernel),
+// for the modes whose interface source needs its gradient; the same
+// stencil and arithmetic as the update kernel's.
+template <typename T, typename S>
+__global__ void __launch_bounds__(kBlock) k_mu(Consts<T> k, State<T, S> s) {
+  const int n = blockIdx.x * kBlock + threadIdx.x;
+  if (n >= k.N) return;
+  int ix, iy, iz;
+  decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
+  const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
+  const Pol pol = Pol::make();
+  const T* __restrict__ pc = s.phi_out;
+  const uint8_t c = s.cls[n];
+  const T phi = ld_pol(pc + n, pol.keep);
+  T ps[Q];
+#pragma unroll
+  for (int q = 1; q < Q; ++q) ps[q] = ld_pol(pc + nb.at(n, ex(q), ey(q), ez(q)), pol.keep);
+  auto solid_at = [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; };
+  T gx, gy, gz, lap;
+  grad_lap<T, true, State<T, S>, decltype(solid_at), true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
+  st_pol(s.mu + n, chem_pot(k, c, phi, lap), pol.keep);
 }
 
 // ---------------------------------------------------------------------------
@@ -1029,7 +1146,7 @@ __device__ __forceinline__ void load_desc(D& dst, const D* src) {
 }
 
 template <typename T, typename S>
-__global__ void __launch_bounds__(kBlock) k_phi_batch(const CaseDesc<T, S>* __restrict__ cases,
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) k_phi_batch(const CaseDesc<T, S>* __restrict__ cases,
                                                      const unsigned short* __restrict__ blk2case) {
   __shared__ CaseDesc<T, S> d;
   load_desc(d, cases + (blk2case ? blk2case[blockIdx.x] : 0));
@@ -1042,15 +1159,15 @@ __global__ void __launch_bounds__(kBlock) k_phi_batch(const CaseDesc<T, S>* __re
   phi_finish(d.s, part, b, nb);
 }
 
-template <typename T, typename S, bool OMEGA1>
-__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_update_batch(
+template <typename T, typename S, bool OMEGA1, bool GMU = false>
+__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S, GMU>::blocks) k_update_batch(
     const CaseDesc<T, S>* __restrict__ cases, const unsigned short* __restrict__ blk2case) {
   __shared__ CaseDesc<T, S> d;
   load_desc(d, cases + (blk2case ? blk2case[blockIdx.x] : 0));
   pdl_trigger();
-  pdl_wait();  // phi of the phi kernel
+  pdl_wait();  // phi of the phi kernel (mu of k_mu with GMU)
   const int n = (blockIdx.x - d.upd_blk0) * kBlock + threadIdx.x;
-  if (n < d.k.N) update_one<T, S, false, false, OMEGA1>(d.k, d.s, n, Pol::make());
+  if (n < d.k.N) update_one<T, S, false, false, OMEGA1, GMU>(d.k, d.s, n, Pol::make());
 }
 
 // Grid of a persistent kernel: resident blocks per SM x SMs (one wave), at
@@ -1151,7 +1268,7 @@ __global__ void __launch_bounds__(kBlock) k_inject(Consts<T> k, State<T, S> s, I
       const T pr = phi;
       phi = clamp01(pr * corr);
       if (k.relax_on && (c & kTop)) {
-        const T r = relax_target(k, pr, corr);
+        const T r = relax_target(k, s.phi_in, s.nsw, n, pr, corr);
         if (r >= T(0)) phi = r;
       }
     }
@@ -1224,7 +1341,7 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
       const T corr = s.cbuf[s.c_cur];
       v = clamp01(phi * corr);
       if (k.relax_on && (c & kTop)) {
-        const T r = relax_target(k, phi, corr);
+        const T r = relax_target(k, (const T*)s.phi_out, s.nsw, n, phi, corr);
         if (r >= T(0)) v = r;
       }
     }
@@ -1417,7 +1534,19 @@ static cudaError_t launch_two_t(const Consts<T>& k, const State<T, S>& s, cudaSt
     e = cudaEventRecord(mid, st);
     if (e != cudaSuccess) return e;
   }
-  k_update<T, S, RAW, FIRST, OMEGA1><<<(k.N + kBlock - 1) / kBlock, kBlock, 0, st>>>(k, s);
+  const int blocks = (k.N + kBlock - 1) / kBlock;
+  if (k.gmu_mode) {
+    // the gradient-of-mu modes: float and double storage, first step here
+    // (later steps run the batched kernels)
+    if constexpr (RAW && FIRST && sizeof(S) != 2) {
+      k_mu<T, S><<<blocks, kBlock, 0, st>>>(k, s);
+      k_update<T, S, RAW, FIRST, OMEGA1, true><<<blocks, kBlock, 0, st>>>(k, s);
+      return cudaGetLastError();
+    } else {
+      return cudaErrorNotSupported;
+    }
+  }
+  k_update<T, S, RAW, FIRST, OMEGA1><<<blocks, kBlock, 0, st>>>(k, s);
   return cudaGetLastError();
 }
 
@@ -1430,6 +1559,7 @@ template <typename T, typename S>
 cudaError_t launch_step(const Consts<T>& k, const State<T, S>& s, const Tiling& tl, bool raw, bool first,
                         cudaStream_t st, cudaEvent_t mid) {
   if (raw != first) return cudaErrorInvalidValue;
+  if (k.gmu_mode && tl.tx != 0) return cudaErrorNotSupported;  // no fused-kernel form of these modes
   if (tl.tx == 0) {
     const bool om1 = k.omega_f == T(1);
     if (raw)
@@ -1475,10 +1605,26 @@ cudaError_t launch_phi_batch(const void* cases, const unsigned short* b2c, int b
 }
 template <typename T, typename S>
 cudaError_t launch_update_batch(const void* cases, const unsigned short* b2c, int blocks, bool omega1,
-                                cudaStream_t st) {
+                                cudaStream_t st, bool gmu) {
   if (blocks <= 0) return cudaSuccess;
-  if (omega1) return launch_pdl(k_update_batch<T, S, true>, blocks, st, static_cast<const CaseDesc<T, S>*>(cases), b2c);
-  return launch_pdl(k_update_batch<T, S, false>, blocks, st, static_cast<const CaseDesc<T, S>*>(cases), b2c);
+  auto c = static_cast<const CaseDesc<T, S>*>(cases);
+  if (gmu) {
+    if constexpr (sizeof(S) != 2) {
+      if (omega1) return launch_pdl(k_update_batch<T, S, true, true>, blocks, st, c, b2c);
+      return launch_pdl(k_update_batch<T, S, false, true>, blocks, st, c, b2c);
+    } else {
+      return cudaErrorNotSupported;
+    }
+  }
+  if (omega1) return launch_pdl(k_update_batch<T, S, true>, blocks, st, c, b2c);
+  return launch_pdl(k_update_batch<T, S, false>, blocks, st, c, b2c);
+}
+// k_mu of one grid (plain stream order: it waits for the phi kernel, and the
+// next update kernel waits for it).
+template <typename T, typename S>
+cudaError_t launch_mu(const Consts<T>& k, const State<T, S>& s, cudaStream_t st) {
+  k_mu<T, S><<<(k.N + kBlock - 1) / kBlock, kBlock, 0, st>>>(k, s);
+  return cudaGetLastError();
 }
 template <typename T, typename S>
 size_t case_desc_bytes() {
@@ -1634,7 +1780,9 @@ LBM_INSTANTIATE(float, __half)
 
 #define LBM_INSTANTIATE_BATCH(T, S)                                                                             \
   template cudaError_t launch_phi_batch<T, S>(const void*, const unsigned short*, int, cudaStream_t);           \
-  template cudaError_t launch_update_batch<T, S>(const void*, const unsigned short*, int, bool, cudaStream_t);  \
+  template cudaError_t launch_update_batch<T, S>(const void*, const unsigned short*, int, bool, cudaStream_t,    \
+                                                 bool);                                                          \
+  template cudaError_t launch_mu<T, S>(const Consts<T>&, const State<T, S>&, cudaStream_t);                     \
   template size_t case_desc_bytes<T, S>();                                                                      \
   template void fill_case_desc<T, S>(void*, const Consts<T>&, const State<T, S>&, int, int, int, int);
 LBM_INSTANTIATE_BATCH(float, float)

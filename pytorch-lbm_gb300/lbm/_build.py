@@ -1,10 +1,11 @@
 """Build liblbm_gb300.so in-tree for sm_103a.
 
-Three translation units compiled in parallel and linked with nvcc:
+Four translation units compiled in parallel and linked with nvcc:
   csrc/lbm_kernels.cu   device kernels (nvcc, sm_103a)
   csrc/lbm_capi.cu      the C ABI of include/lbm_gb300.h (nvcc host code)
   csrc/lbm_geometry.cpp host geometry precompute (g++, -ffp-contract=off so
                         the float sequences match numpy bit for bit)
+  csrc/lbm_io.cpp       host output (the ASCII VTK writer)
 Output: lbm/_lib/liblbm_gb300.so next to this file.
 """
 import os
@@ -55,9 +56,10 @@ def build(force=False, verbose=False):
         obj = os.path.join(obj_dir, src + ".o")
         jobs.append([nvcc, *common, *ARCH, "-lineinfo", "-Xcompiler", HOST_FLAGS, "-c",
                      os.path.join(CSRC, src), "-o", obj])
-    obj = os.path.join(obj_dir, "lbm_geometry.cpp.o")
-    jobs.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
-                 "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, "lbm_geometry.cpp"), "-o", obj])
+    for src in ("lbm_geometry.cpp", "lbm_io.cpp"):
+        obj = os.path.join(obj_dir, src + ".o")
+        jobs.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
+                     "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -70,7 +72,7 @@ def build(force=False, verbose=False):
         list(ex.map(run, jobs))
     objs = [j[-1] for j in jobs]
     tmp = LIB + ".tmp"
-    run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

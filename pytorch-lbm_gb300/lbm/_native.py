@@ -17,6 +17,7 @@ LBM_F32, LBM_F64, LBM_F16 = 0, 1, 2
 LBM_DT_NONE, LBM_DT_F32, LBM_DT_F64 = 0, 1, 2
 FIELD_PHI, FIELD_RHO, FIELD_U, FIELD_P, FIELD_PRESS, FIELD_MU = 1, 2, 4, 8, 16, 32
 STATUS_NAN, STATUS_MASS_LOW = 1, 2
+IFACE_ALLEN_CAHN, IFACE_CAHN_HILLIARD = 0, 1
 
 # every exported entry point declared in include/lbm_gb300.h
 EXPORTS = (
@@ -25,7 +26,8 @@ EXPORTS = (
     "lbm_get_scalars", "lbm_measure", "lbm_status", "lbm_last_error", "lbm_version",
     "lbm_set_tile", "lbm_get_tile", "lbm_autotune", "lbm_measure_static", "lbm_footprint",
     "lbm_batch_create", "lbm_batch_step", "lbm_batch_size", "lbm_batch_autotune", "lbm_batch_destroy",
-    "lbm_inject_droplet",
+    "lbm_inject_droplet", "lbm_set_amplification", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
+    "lbm_write_vtk",
 )
 
 
@@ -39,7 +41,8 @@ class LbmParams(ctypes.Structure):
         ("sharpen_reduce", ctypes.c_double), ("mu_wall_scale", ctypes.c_double),
         ("geo_amplification", ctypes.c_double), ("ac_scale", ctypes.c_double),
         ("ghost_scale", ctypes.c_double), ("stab_mode", ctypes.c_int32),
-        ("geometric_wetting", ctypes.c_int32),
+        ("geometric_wetting", ctypes.c_int32), ("interface_mode", ctypes.c_int32),
+        ("direct_wetting", ctypes.c_int32), ("mu_drive", ctypes.c_double),
     ]
 
 
@@ -73,6 +76,11 @@ def _declare(L):
         "lbm_batch_destroy": ([_vp], _i32),
         "lbm_inject_droplet": ([_vp, ctypes.POINTER(_dbl), _dbl, _dbl, ctypes.POINTER(_dbl), ctypes.POINTER(_i64),
                                 _vp], _i32),
+        "lbm_set_amplification": ([_vp, _vp, _i32], _i32),
+        "lbm_state_bytes": ([_vp, ctypes.POINTER(_i64)], _i32),
+        "lbm_save_state": ([_vp, _vp, _i64, _vp], _i32),
+        "lbm_load_state": ([_vp, _vp, _i64, _vp], _i32),
+        "lbm_write_vtk": ([ctypes.c_char_p, ctypes.c_char_p, _i64, _vp, _vp, _vp, _vp, _vp], _i32),
         "lbm_status": ([_vp, ctypes.POINTER(_u32)], _i32),
         "lbm_set_tile": ([_vp, _i32, _i32, _i32], _i32),
         "lbm_get_tile": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),

@@ -13,9 +13,11 @@ needs (post-collision populations, velocity, the previous phi) and a read of
 ``solver.phi`` etc. launches a small read-out kernel that reproduces the value
 the reference holds after the same step.  Each read returns a new tensor.
 
-Options the reference implements but this solver does not yet cover
-(``interface_mode='cahn-hilliard'``, ``mu_drive > 0``, ``direct_wetting``,
-per-node ``geo_amplification`` tensors, 2-D grids) raise
+``geo_amplification`` may be a scalar or a per-node field of the grid's shape
+(torch tensor or numpy array), as in the reference.  ``interface_mode=
+'cahn-hilliard'`` and ``mu_drive > 0`` add a chemical-potential pass per step
+(float32 / float64); ``direct_wetting`` relaxes top-surface boundary phi towards
+the cubic-wall-energy value.  2-D grids (the reference's D2Q9 path) raise
 ``NotImplementedError`` instead of running a different model.
 """
 from __future__ import annotations
@@ -79,14 +81,16 @@ class AllenCahnSolver:
                  direct_wetting=False, ch_wall_blend=0.0, geo_amplification=1.0, ac_scale=1.0):
         if config.nz == 1:
             raise NotImplementedError("2-D (D2Q9) grids are not supported by the GB300 solver")
-        if interface_mode != "allen-cahn":
-            raise NotImplementedError("interface_mode='cahn-hilliard' is not supported")
-        if mu_drive and mu_drive > 0.0:
-            raise NotImplementedError("mu_drive > 0 is not supported")
-        if direct_wetting:
-            raise NotImplementedError("direct_wetting is not supported")
+        if interface_mode not in ("allen-cahn", "cahn-hilliard"):
+            raise ValueError(f"unknown interface_mode {interface_mode!r}")
+        if (interface_mode == "cahn-hilliard" or mu_drive > 0.0) and dtype == torch.float16:
+            raise NotImplementedError("interface_mode='cahn-hilliard' and mu_drive > 0 need float32 or float64")
+        amp_field = None
         if torch.is_tensor(geo_amplification) or isinstance(geo_amplification, np.ndarray):
-            raise NotImplementedError("per-node geo_amplification is not supported")
+            # per-node field (lbm/fe_wetting.py:503-512)
+            amp_field = _host_array(geo_amplification, np.float64)
+            if amp_field.shape != tuple(config.grid_shape):
+                raise ValueError(f"geo_amplification field shape {amp_field.shape} != grid {tuple(config.grid_shape)}")
         if dtype not in (torch.float32, torch.float64, torch.float16):
             raise ValueError("dtype must be torch.float32, torch.float64 or torch.float16")
         self.config = config
@@ -147,11 +151,14 @@ class AllenCahnSolver:
         p.boundary_relax = float(boundary_relax)
         p.sharpen_reduce = float(sharpen_reduce)
         p.mu_wall_scale = float(mu_wall_scale)
-        p.geo_amplification = float(geo_amplification)
+        p.geo_amplification = 1.0 if amp_field is not None else float(geo_amplification)
         p.ac_scale = float(ac_scale)
         p.ghost_scale = float(ghost_scale) if ghost_scale is not None else 0.0
         p.stab_mode = _STAB[self.stab_mode]
         p.geometric_wetting = 1 if geometric_wetting else 0
+        p.interface_mode = nat.IFACE_CAHN_HILLIARD if interface_mode == "cahn-hilliard" else nat.IFACE_ALLEN_CAHN
+        p.mu_drive = float(mu_drive)
+        p.direct_wetting = 1 if direct_wetting else 0
         self._params = p
         self._lib = nat.lib()
         h = ctypes.c_void_p()
@@ -159,6 +166,9 @@ class AllenCahnSolver:
             nat.check(self._lib.lbm_create(ctypes.byref(p), self.shape[0], self.shape[1], self.shape[2],
                                            self._prec, ctypes.byref(h)), "lbm_create")
         self._h = h
+        if amp_field is not None:
+            nat.check(self._lib.lbm_set_amplification(h, amp_field.ctypes.data_as(ctypes.c_void_p), nat.LBM_DT_F64),
+                      "lbm_set_amplification")
         self._geometry_set = False
         self._initialized = False
         self._cache = {}
@@ -413,6 +423,67 @@ class AllenCahnSolver:
         t = (ctypes.c_int * 3)()
         nat.check(self._lib.lbm_get_tile(self._h, t), "lbm_get_tile")
         return tuple(t)
+
+    # -- checkpoints and snapshots ---------------------------------------------
+    def state_dict(self):
+        """The complete time-stepping state as host data: resuming from it
+        (``load_state_dict`` on a solver built with the same config, options,
+        precision and geometry) continues bit-identically.  The reference has
+        no counterpart; this is what its long runs lacked for restarts."""
+        if not self._initialized:
+            raise RuntimeError("state_dict is defined after init_fields")
+        n = ctypes.c_int64()
+        nat.check(self._lib.lbm_state_bytes(self._h, ctypes.byref(n)), "lbm_state_bytes")
+        buf = np.empty(n.value, dtype=np.uint8)
+        nat.check(self._lib.lbm_save_state(self._h, buf.ctypes.data_as(ctypes.c_void_p), n.value, nat.stream_ptr()),
+                  "lbm_save_state")
+        return {"format": "lbm_gb300.state.v1", "grid": tuple(self.shape),
+                "precision": str(self.population_dtype).replace("torch.", ""),
+                "step_count": int(self.step_count), "t": float(self.t), "state": buf}
+
+    def load_state_dict(self, state):
+        """Restore a ``state_dict`` (after ``set_solid`` with the same geometry)."""
+        if not self._geometry_set:
+            raise RuntimeError("call set_solid (the same geometry) before load_state_dict")
+        if str(state["format"]) != "lbm_gb300.state.v1":
+            raise ValueError(f"unknown state format {state['format']!r}")
+        buf = np.ascontiguousarray(state["state"], dtype=np.uint8)
+        nat.check(self._lib.lbm_load_state(self._h, buf.ctypes.data_as(ctypes.c_void_p), buf.size, nat.stream_ptr()),
+                  "lbm_load_state")
+        self.step_count = int(state["step_count"])
+        self.t = float(state["t"])
+        self._initialized = True
+        self._cache.clear()
+
+    def save_checkpoint(self, path):
+        """``state_dict`` to an ``.npz`` file."""
+        sd = self.state_dict()
+        np.savez(path, format=np.array(sd["format"]), grid=np.array(sd["grid"]), precision=np.array(sd["precision"]),
+                 step_count=np.array(sd["step_count"]), t=np.array(sd["t"]), state=sd["state"])
+
+    def load_checkpoint(self, path):
+        """Restore a checkpoint written by ``save_checkpoint``."""
+        with np.load(path) as z:
+            grid = tuple(int(x) for x in z["grid"])
+            if grid != tuple(self.shape):
+                raise ValueError(f"checkpoint grid {grid} != solver grid {tuple(self.shape)}")
+            self.load_state_dict({"format": str(z["format"]), "step_count": int(z["step_count"]),
+                                  "t": float(z["t"]), "state": z["state"]})
+
+    def save_snapshot(self, path, step=None):
+        """Compressed ``.npz`` snapshot of phi, u and the solid mask with the
+        mid-plane slices, in the key layout of the reference's sweep driver
+        (scripts/run_thesis_sweep.py:219-243): phi_3d, u_3d, solid_3d, xz_slice,
+        yz_slice, xz_solid, step, nx, ny, nz."""
+        phi, vel = self.fields("phi", "u")
+        phi_np = phi.detach().cpu().numpy()
+        u_np = vel.detach().cpu().numpy()
+        solid_np = self.solid.cpu().numpy()
+        nx, ny, nz = self.shape
+        np.savez_compressed(path, phi_3d=phi_np, u_3d=u_np, solid_3d=solid_np,
+                            xz_slice=phi_np[:, ny // 2, :], yz_slice=phi_np[nx // 2, :, :],
+                            xz_solid=solid_np[:, ny // 2, :],
+                            step=self.step_count if step is None else step, nx=nx, ny=ny, nz=nz)
 
     def status(self):
         v = ctypes.c_uint32()

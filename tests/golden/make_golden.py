@@ -24,6 +24,17 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
+
+def alpha_ramp(grid, lo, hi):
+    """Per-node geometric amplification field rising linearly in x from lo to
+    hi (float32): part of the wall has alpha <= 1 (amplification off there),
+    part alpha > 1, as in the adaptive-alpha runs of
+    scripts/adaptive_alpha_study.py:157-160."""
+    nx, ny, nz = grid
+    ramp = (np.float32(lo) + np.float32(hi - lo) * np.arange(nx, dtype=np.float32) / np.float32(nx - 1))
+    return np.ascontiguousarray(np.broadcast_to(ramp[:, None, None], (nx, ny, nz)), dtype=np.float32)
+
+
 # name: grid, substrate, droplet, solver kwargs, config overrides, dtypes, checkpoints
 CASES = {
     # Short runs (steps 1 and 5) on small grids: every stage's output at step 1.
@@ -46,6 +57,26 @@ CASES = {
     "discrete_l162": dict(
         grid=(32, 32, 28), substrate=("mask", "ridge", 1.0, 6.0), drop=dict(center=(16, 16, 15), radius=6.0, u=(0, 0, -0.05)),
         cfg=dict(theta_eq=162.0), kw=dict(geo_amplification=1.8, geometric_wetting=True, boundary_relax=0.0),
+        dtypes=("float32",), ckpt=(1, 5), save_f=False),
+    "ridge_alpha_field": dict(
+        grid=(32, 32, 28), substrate=("fraction", "ridge", 1.0, 6.0), drop=dict(center=(16, 16, 15), radius=6.0, u=(0, 0, -0.05)),
+        cfg=dict(theta_eq=162.0), kw=dict(geo_amplification=alpha_ramp((32, 32, 28), 0.6, 2.4), geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "ch_flat_q120": dict(
+        grid=(24, 24, 20), substrate=("flat_z2",), drop=dict(center=(12, 12, 7), radius=6.0, u=(0, 0, -0.01)),
+        cfg=dict(theta_eq=120.0), kw=dict(interface_mode="cahn-hilliard", geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "mudrive_ridge_l150": dict(
+        grid=(32, 32, 28), substrate=("fraction", "ridge", 1.0, 6.0), drop=dict(center=(16, 16, 15), radius=6.0, u=(0, 0, -0.05)),
+        cfg=dict(theta_eq=150.0), kw=dict(mu_drive=0.5, geo_amplification=1.5, geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "direct_ridge_l150": dict(
+        grid=(32, 32, 28), substrate=("fraction", "ridge", 1.0, 6.0), drop=dict(center=(16, 16, 11), radius=6.0, u=(0, 0, -0.05)),
+        cfg=dict(theta_eq=150.0), kw=dict(direct_wetting=True, geo_amplification=1.5, geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "direct_flat_q120": dict(
+        grid=(24, 24, 20), substrate=("flat_z2",), drop=dict(center=(12, 12, 7), radius=6.0, u=(0, 0, 0)),
+        cfg=dict(theta_eq=120.0), kw=dict(direct_wetting=True, boundary_relax=0.5),
         dtypes=("float32",), ckpt=(1, 5), save_f=False),
     "nowet_liang_grav": dict(
         grid=(24, 24, 20), substrate=("flat_z2",), drop=dict(center=(12, 12, 8), radius=5.0, u=(0, 0, -0.02)),
@@ -99,8 +130,10 @@ def run_case(ref, name, case, dtype_name):
     solid, frac, C, u = build_inputs(ref, case)
     dt = getattr(torch, dtype_name)
     out = {}
+    # a per-node amplification field goes to the reference as a torch tensor
+    kw = {k: (torch.from_numpy(v) if isinstance(v, np.ndarray) else v) for k, v in case["kw"].items()}
     with contextlib.redirect_stdout(io.StringIO()):
-        s = ref["Solver"](cfg, dtype=dt, **case["kw"])
+        s = ref["Solver"](cfg, dtype=dt, **kw)
         s.set_solid(solid, solid_fraction=frac)
         s.init_fields(C, u)
     out["solid"] = np.asarray(solid, dtype=bool)

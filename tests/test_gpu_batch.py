@@ -107,3 +107,36 @@ def test_injected_case_in_batch_matches_alone():
     for x, y in zip(a, m):
         for p, q in zip(_state(x), _state(y)):
             assert torch.equal(p, q)
+
+
+def test_batch_with_amplification_field():
+    """A case with a per-node amplification field gives the same results alone
+    and in a batch (its descriptor carries the field)."""
+    from lbm.batch import AllenCahnBatch
+    from lbm.fe_ac_solver import AllenCahnSolver
+
+    def make(case, field):
+        cfg = impact_config(case, "cuda")
+        solid, frac, C, u = impact_inputs(case)
+        amp = 1.5
+        if field:
+            nx, ny, nz = case.grid
+            amp = np.broadcast_to(np.linspace(0.5, 2.5, nx, dtype=np.float32)[:, None, None], (nx, ny, nz)).copy()
+        s = AllenCahnSolver(cfg, dtype=torch.float32, geo_amplification=amp, geometric_wetting=True)
+        s.set_solid(solid, frac)
+        s.init_fields(C, u)
+        return s
+
+    alone = [make(CASES[1], True), make(CASES[3], False)]
+    for s in alone:
+        s.run(6)
+    mixed = [make(CASES[1], True), make(CASES[3], False)]
+    b = AllenCahnBatch(mixed)
+    b.run(6)
+    for a, m in zip(alone, mixed):
+        for x, y in zip(_state(a), _state(m)):
+            assert torch.equal(x, y)
+    # the field changes the result (it is not ignored)
+    plain = make(CASES[1], False)
+    plain.run(6)
+    assert not torch.equal(plain.phi, alone[0].phi)

@@ -160,9 +160,22 @@ def test_api_errors():
     s = AllenCahnSolver(cfg, dtype=torch.float32)
     with pytest.raises(RuntimeError):
         s.step()
-    for kw in (dict(interface_mode="cahn-hilliard"), dict(mu_drive=0.1), dict(direct_wetting=True),
-               dict(geo_amplification=torch.ones(16, 16, 12))):
+    # the gradient-of-mu modes: float32 / float64 only, two-kernel step only, not batched
+    from lbm import _native as nat
+    from lbm.batch import AllenCahnBatch
+    for kw in (dict(interface_mode="cahn-hilliard"), dict(mu_drive=0.1)):
         with pytest.raises(NotImplementedError):
-            AllenCahnSolver(cfg, **kw)
+            AllenCahnSolver(cfg, dtype=torch.float16, **kw)
+        ch = AllenCahnSolver(cfg, dtype=torch.float32, **kw)
+        ch.set_solid(np.zeros((16, 16, 12), bool))
+        ch.init_fields(np.full((16, 16, 12), 0.5, np.float32))
+        with pytest.raises(nat.LbmError):
+            ch.set_tile(4, 4, 6)
+        with pytest.raises(nat.LbmError):
+            AllenCahnBatch([ch])
+    with pytest.raises(ValueError):
+        AllenCahnSolver(cfg, interface_mode="phase-field")
+    with pytest.raises(ValueError):  # a per-node amplification field must have the grid's shape
+        AllenCahnSolver(cfg, geo_amplification=torch.ones(16, 16, 11))
     with pytest.raises(ValueError):
         s.set_solid(np.zeros((4, 4, 4), bool))
