@@ -263,7 +263,7 @@ def run_ours(args, rank, world, device):
     meas = s.measure()
     if status & nat.STATUS_NAN or meas["has_nan"]:
         raise RuntimeError("NaN in the benchmark run")
-    value = world * n * K / (tot_ms / 1e3) / 1e6
+    value = replica_mlups(n, K, tot_ms, world)
 
     # --- end to end through the public API from host arrays ----------------
     torch.cuda.synchronize(device)
@@ -282,7 +282,7 @@ def run_ours(args, rank, world, device):
     torch.cuda.synchronize(device)
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world, device)
-    e2e = world * n * K / e2e_s / 1e6
+    e2e = replica_mlups(n, K, e2e_s * 1e3, world)
     h2d = solid.nbytes + frac.nbytes + C.nbytes + u.nbytes
     d2h = reads * n * 4 + 9 * 8
 
@@ -449,6 +449,12 @@ def barrier(world):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+def replica_mlups(nodes, steps, ms, world):
+    """Whole-job MLUPS of `world` independent replicas that each advance a
+    grid of `nodes` nodes by `steps` steps; `ms` is the slowest rank's time."""
+    return world * nodes * steps / (ms / 1e3) / 1e6
 
 
 def max_over_ranks(x, world, device):

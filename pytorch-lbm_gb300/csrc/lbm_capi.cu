@@ -43,6 +43,7 @@ template <typename T, typename S>
 cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, cudaStream_t, bool = false);
 template <typename T, typename S>
 cudaError_t launch_mu(const Consts<T>&, const State<T, S>&, cudaStream_t);
+
 template <typename T, typename S>
 size_t case_desc_bytes();
 template <typename T, typename S>
@@ -92,6 +93,7 @@ struct LbmHandle {
   void* amp = nullptr;           // N x T per-node geometric amplification (lbm_set_amplification), or null
   void* mu = nullptr;            // Np x T chemical potential of the step (gradient-of-mu modes only)
   int* nsw = nullptr;            // N next-interior node indices (direct wetting only)
+  void* cubic = nullptr;         // 4 x T cubic-wall-energy constants (direct wetting only)
   // derived
   bool wetting = false;
   Consts<float> kf{};
@@ -193,7 +195,6 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   k.amp = (T)p.geo_amplification;
   // boundary-phi relaxation target (fe_ac_solver.py:165-177, 613-616)
   k.relax_on = 0;
-  k.direct = 0;
   if (k.wetting && p.boundary_relax > 0 && p.theta_eq != 90.0) {
     const double c = std::cos(th);
     const double disc = 1.0 - 4.0 * (-c / 3.0);
@@ -201,16 +202,9 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
     if (disc >= 0) target = 0.5 * (1.0 - std::sqrt(disc));
     else target = 0.5 * (1.0 - std::cos(M_PI - th));
     if (p.direct_wetting) {
-      // cubic wall energy (fe_ac_solver.py:609-612, fe_wetting.py:369-416)
-      const double a = 6.0 * p.sigma * c / p.kappa, oma = 1.0 - a;
+      // cubic wall energy (fe_ac_solver.py:609-612); its constants: cubic_consts
       k.relax_on = 1;
-      k.direct = 1;
       k.relax_r = (T)p.boundary_relax;
-      k.cubic_on = std::fabs(a) >= 1e-10 ? 1 : 0;
-      k.cub_oma2 = (T)(oma * oma);
-      k.cub_four_a = (T)(4.0 * a);
-      k.cub_neg_oma = (T)(-oma);
-      k.cub_two_a = (T)(2.0 * a);
     } else if (std::fabs(target - 0.5) > 0.05) {
       k.relax_on = 1;
       k.relax_target = (T)target;
@@ -225,6 +219,18 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   k.guo = (T)(tau_f / (tau_f - 0.5));
   k.mu_drive_a = (T)(p.mu_drive * mob);
   return k;
+}
+
+// Constants of the cubic-wall-energy boundary phi (fe_wetting.py:369-416) in
+// the compute type: (1 - a)^2, 4 a, -(1 - a), 2 a, a = 6 sigma cos(theta) /
+// kappa; 2 a = 0 when |a| < 1e-10 (no correction).
+template <typename T>
+void cubic_consts(const LbmParams& p, T* out4) {
+  const double a = 6.0 * p.sigma * std::cos(p.theta_eq * M_PI / 180.0) / p.kappa, oma = 1.0 - a;
+  out4[0] = (T)(oma * oma);
+  out4[1] = (T)(4.0 * a);
+  out4[2] = (T)(-oma);
+  out4[3] = std::fabs(a) >= 1e-10 ? (T)(2.0 * a) : (T)0;
 }
 
 // The constant table holds the same lattice values the kernels may also use
@@ -271,6 +277,7 @@ State<T, S> make_state(const LbmHandle& h, int in_buf, int phi_in) {
   s.amp = static_cast<const T*>(h.amp);
   s.mu = static_cast<T*>(h.mu);
   s.nsw = h.nsw;
+  s.cubic = static_cast<const T*>(h.cubic);
   s.partials = h.partials;
   s.counter = h.counters;
   s.cbuf = static_cast<T*>(h.cbuf);
@@ -325,7 +332,7 @@ Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz, i
 void free_all(LbmHandle* h) {
   void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u,        h->phi[0], h->phi[1], h->eps,
                   h->cls,  h->wn,   h->partials, h->counters, h->cbuf, h->scal, h->meas_phi, h->desc,
-                  h->amp,  h->mu, h->nsw};
+                  h->amp,  h->mu, h->nsw, h->cubic};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -385,10 +392,10 @@ int launch_next(LbmHandle* h, const Tiling& t, cudaStream_t st, cudaEvent_t mid)
       if (rc != LBM_OK) return rc;
     }
     const int par = (h->cur ^ h->desc_cur0) & 1;
+    const bool gmu = h->mu != nullptr;
     const unsigned char* d = static_cast<const unsigned char*>(h->desc) + par * case_desc_bytes<T, S>();
     CUDA_TRY((launch_phi_batch<T, S>(d, nullptr, phi_blocks_of(h, h->phi_per_thread), st)));
     if (mid) CUDA_TRY(cudaEventRecord(mid, st));
-    const bool gmu = h->mu != nullptr;
     if (gmu) {
       State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
       CUDA_TRY((launch_mu<T, S>(consts_of<T>(*h), s, st)));
@@ -575,9 +582,19 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
   const int64_t N = h->N;
   CUDA_TRY(cudaMemcpy(h->cls, h->geo.cls.data(), N, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(h->wn, h->geo.wall_normal.data(), 3 * N * sizeof(float), cudaMemcpyHostToDevice));
-  if (h->prm.direct_wetting) {
+  if (h->prm.direct_wetting && h->wetting && h->prm.boundary_relax > 0) {
     if (!h->nsw) CUDA_TRY(cudaMalloc(&h->nsw, N * sizeof(int)));
     CUDA_TRY(cudaMemcpy(h->nsw, h->geo.nsw.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    if (!h->cubic) CUDA_TRY(cudaMalloc(&h->cubic, 4 * sizeof(double)));
+    if (h->prec == LBM_F64) {
+      double c4[4];
+      cubic_consts(h->prm, c4);
+      CUDA_TRY(cudaMemcpy(h->cubic, c4, sizeof(c4), cudaMemcpyHostToDevice));
+    } else {
+      float c4[4];
+      cubic_consts(h->prm, c4);
+      CUDA_TRY(cudaMemcpy(h->cubic, c4, sizeof(c4), cudaMemcpyHostToDevice));
+    }
   }
   if (h->prec != LBM_F64) {
     std::vector<float> eps(N, 0.0f);

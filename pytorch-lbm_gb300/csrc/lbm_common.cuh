@@ -163,10 +163,6 @@ struct Consts {
   T mu_wall_add;         // mu_wall * mu_wall_scale (linear)
   T cos_t, sin_t, amp;
   T relax_r, relax_target;
-  // cubic-wall-energy boundary phi (direct wetting, fe_wetting.py:369-416):
-  // target root of a phi_b^2 + (1 - a) phi_b - phi_nsw = 0, a = 6 sigma cos(theta) / kappa
-  int direct, cubic_on;
-  T cub_oma2, cub_four_a, cub_neg_oma, cub_two_a;  // (1 - a)^2, 4 a, -(1 - a), 2 a
   T ww[16];              // near-wall weight by code (float32 values)
   // chemical-potential gradient terms of the interface source
   // (lbm/fe_ac_solver.py:457-486): 0 none, kGmuCH Cahn-Hilliard, kGmuDrive mu_drive
@@ -193,6 +189,10 @@ struct State {
   const T* amp;     // per-node geometric amplification (read at boundary nodes only; null: the scalar k.amp)
   T* mu;            // chemical potential of this step [N] (k_mu; the gradient-of-mu modes only)
   const int* nsw;   // next-interior fluid node of a boundary node or -1 [N] (direct wetting only)
+  // direct wetting (cubic wall energy, fe_wetting.py:369-416), null when off:
+  // (1 - a)^2, 4 a, -(1 - a), 2 a with a = 6 sigma cos(theta) / kappa (2 a = 0: no cubic root).
+  // Kept out of Consts: the step kernels' register allocation is sensitive to its size.
+  const T* cubic;
   double* partials; // one per block
   unsigned* counter;
   T* cbuf;          // mass-correction factor of the last two steps

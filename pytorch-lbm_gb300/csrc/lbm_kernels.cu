@@ -274,18 +274,19 @@ __device__ __forceinline__ T seqsum(const T (&v)[Q]) {
 // the node's own phi where that does not apply.
 template <typename T>
 __device__ __forceinline__ T relax_target(const Consts<T>& k, const T* __restrict__ phi_arr,
-                                          const int* __restrict__ nsw, int n, T phi_prev, T corr) {
+                                          const int* __restrict__ nsw, const T* __restrict__ cubic, int n, T phi_prev,
+                                          T corr) {
   const T pb = clamp01(phi_prev * corr);
   if (!(pb > T(0.15) && pb < T(0.85))) return T(-1);
   T target = k.relax_target;
-  if (k.direct) {
+  if (cubic) {
     target = pb;
     const int m = nsw[n];
-    if (k.cubic_on && m >= 0 && pb > T(0.01) && pb < T(0.99)) {
+    if (m >= 0 && cubic[3] != T(0) && pb > T(0.01) && pb < T(0.99)) {
       const T pn = clamp01(phi_arr[m] * corr);
-      T disc = k.cub_oma2 + k.cub_four_a * pn;
+      T disc = cubic[0] + cubic[1] * pn;
       disc = disc < T(0) ? T(0) : disc;
-      target = clamp01((k.cub_neg_oma + sqrt(disc)) / k.cub_two_a);
+      target = clamp01((cubic[2] + sqrt(disc)) / cubic[3]);
     }
   }
   return clamp01(pb + k.relax_r * (target - pb));
@@ -306,7 +307,7 @@ __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const Sta
   const T corr = RAW ? T(1) : s.cbuf[s.c_prev];
   fetch_pop<T, S, RAW, !RAW, true, USE_POL>(v, k, s.fin, s.phi_in, n, N, nb, c, eps, corr, pol);
   if (!RAW && k.relax_on && (c & kTop)) {
-    const T r = relax_target(k, s.phi_in, s.nsw, n, ldg(s.phi_in + n), corr);
+    const T r = relax_target(k, s.phi_in, s.nsw, s.cubic, n, ldg(s.phi_in + n), corr);
     if (r >= T(0)) {
       const T sc = relax_scale(r, seqsum(v));
 #pragma unroll
@@ -554,14 +555,14 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     T tm = sqrt(add_rn(add_rn(mul_rn(tx, tx), mul_rn(ty, ty)), mul_rn(tz, tz)));
     tm = tm < T(1e-10) ? T(1e-10) : tm;
     T gd = mul_rn(-tm, k.cos_t) / k.sin_t;
+    // scalar amplification, or a per-node field active where alpha > 1 (fe_wetting.py:503-512)
+    T a = k.amp;
+    bool amp_on = k.amp_active;
     if (s.amp) {
-      // per-node amplification field: active where alpha > 1 (fe_wetting.py:503-512)
-      const T a = s.amp[n];
-      if (a > T(1)) gd = add_rn(gn, mul_rn(gd - gn, a));
-    } else if (k.amp_active) {
-      const T delta = gd - gn;
-      gd = add_rn(gn, mul_rn(delta, k.amp));
+      a = s.amp[n];
+      amp_on = a > T(1);
     }
+    if (amp_on) gd = add_rn(gn, mul_rn(gd - gn, a));
     const T cx = add_rn(tx, mul_rn(gd, n0)), cy = add_rn(ty, mul_rn(gd, n1)), cz = add_rn(tz, mul_rn(gd, n2));
     const T gm = sqrt(add_rn(add_rn(mul_rn(gx, gx), mul_rn(gy, gy)), mul_rn(gz, gz)));
     if (gm > T(1e-6)) {
@@ -1268,7 +1269,7 @@ __global__ void __launch_bounds__(kBlock) k_inject(Consts<T> k, State<T, S> s, I
       const T pr = phi;
       phi = clamp01(pr * corr);
       if (k.relax_on && (c & kTop)) {
-        const T r = relax_target(k, s.phi_in, s.nsw, n, pr, corr);
+        const T r = relax_target(k, s.phi_in, s.nsw, s.cubic, n, pr, corr);
         if (r >= T(0)) phi = r;
       }
     }
@@ -1341,7 +1342,7 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
       const T corr = s.cbuf[s.c_cur];
       v = clamp01(phi * corr);
       if (k.relax_on && (c & kTop)) {
-        const T r = relax_target(k, (const T*)s.phi_out, s.nsw, n, phi, corr);
+        const T r = relax_target(k, (const T*)s.phi_out, s.nsw, s.cubic, n, phi, corr);
         if (r >= T(0)) v = r;
       }
     }
