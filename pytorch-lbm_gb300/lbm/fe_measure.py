@@ -1,0 +1,128 @@
+"""Droplet measurements with the reference's functions and return values
+(pytorch-lbm ``lbm/fe_measure.py``): spread factors and the wall contact angle.
+
+``measure_spread_factor`` reduces a CUDA field on the device (the library's
+allocation-free spread reduction, ``lbm_measure_static``), so a caller that
+polls a running solve copies 9 numbers to the host instead of the field;
+host arrays and 2-D fields are measured on the host.  ``measure_contact_angle``
+scans one wall layer and one column, which the reference does on the host;
+it stays there.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+try:
+    import torch
+except ImportError:  # pragma: no cover - torch is part of the package's requirements
+    torch = None
+
+
+def _host(x):
+    if torch is not None and isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
+
+
+def _empty(volume, c_max):
+    return {"Dx": 0.0, "Dy": 0.0, "Dz": 0.0, "k": 0.0, "volume": volume, "C_max": c_max}
+
+
+def _spread_device(C, solid_mask):
+    from . import _native as nat
+    nx, ny, nz = C.shape
+    phi = C.detach().contiguous()
+    if phi.dtype not in (torch.float32, torch.float64):
+        phi = phi.to(torch.float32)
+    if solid_mask is None:
+        solid = torch.zeros(C.shape, dtype=torch.uint8, device=C.device)
+    else:
+        solid = torch.as_tensor(solid_mask, device=C.device).to(torch.bool).contiguous().view(torch.uint8)
+    out = torch.empty(9, dtype=torch.float64, device=C.device)
+    dt = nat.LBM_DT_F32 if phi.dtype == torch.float32 else nat.LBM_DT_F64
+    with torch.cuda.device(C.device):
+        nat.check(nat.lib().lbm_measure_static(nx, ny, nz, nat.ptr(phi), dt, ctypes.c_void_p(solid.data_ptr()),
+                                               nat.ptr(out), nat.stream_ptr()), "lbm_measure_static")
+        v = out.cpu().numpy()
+    volume, c_max, count = float(v[0]), float(v[1]), int(v[7])
+    if count == 0:
+        return _empty(volume, c_max)
+    Dx, Dy, Dz = float(v[2]), float(v[3]), float(v[4])
+    return {"Dx": Dx, "Dy": Dy, "Dz": Dz, "k": Dx / Dy if Dy > 0 else 0.0, "volume": volume, "C_max": c_max}
+
+
+def measure_spread_factor(C, solid_mask=None) -> dict:
+    """Extents Dx, Dy, Dz of the C > 0.5 set (solid nodes excluded), k = Dx / Dy,
+    volume = sum of C with solid nodes zeroed, C_max (lbm/fe_measure.py:11-82).
+
+    A 3-D CUDA tensor is reduced on its device (the volume summed in float64);
+    anything else on the host."""
+    if torch is not None and isinstance(C, torch.Tensor) and C.is_cuda and C.dim() == 3:
+        return _spread_device(C, solid_mask)
+    c = np.array(_host(C), copy=True)
+    if solid_mask is not None:
+        c[_host(solid_mask).astype(bool)] = 0.0
+    volume = float(c.sum())
+    c_max = float(c.max())
+    inside = c > 0.5
+    if not inside.any():
+        return _empty(volume, c_max)
+    ext = []
+    for axis in range(c.ndim):
+        other = tuple(a for a in range(c.ndim) if a != axis)
+        hit = np.flatnonzero(inside.any(axis=other))
+        ext.append(float(hit[-1] - hit[0] + 1))
+    Dx, Dy = ext[0], ext[1]
+    Dz = ext[2] if c.ndim == 3 else 0.0
+    return {"Dx": Dx, "Dy": Dy, "Dz": Dz, "k": Dx / Dy if Dy > 0 else 0.0, "volume": volume, "C_max": c_max}
+
+
+def _contact_angle(c, solid):
+    """Contact angle (degrees) from the last axis' first fluid layer above the
+    wall, as lbm/fe_measure.py:132-241: the contact-region point farthest from
+    the domain's centre axis gives the contact radius r; the height h of the
+    C = 0.5 crossing above the wall top in that column (linear interpolation,
+    at least 0.5) gives theta = atan2(r, h).  180 when there is no contact."""
+    n_last = c.shape[-1]
+    wall_top = 0
+    for z in range(n_last):
+        if not solid[..., z].all():
+            wall_top = z
+            break
+    first = wall_top + 1
+    if first >= n_last:
+        return 180.0
+    layer = c[..., first] > 0.5
+    if not layer.any():
+        return 180.0
+    pts = np.argwhere(layer)
+    centre = np.array([s / 2.0 for s in c.shape[:-1]])
+    if c.ndim == 2:
+        radii = np.abs(pts[:, 0] - centre[0])
+    else:
+        radii = np.sqrt((pts[:, 0] - centre[0]) ** 2 + (pts[:, 1] - centre[1]) ** 2)
+    i = int(np.argmax(radii))
+    r = radii[i]
+    if r < 1.0:
+        return 180.0
+    col = c[tuple(pts[i])]
+    h = None
+    for z in range(first, n_last - 1):
+        if col[z] >= 0.5 and col[z + 1] < 0.5:
+            h = z + (col[z] - 0.5) / (col[z] - col[z + 1] + 1e-10)
+            break
+    if h is None:
+        return 180.0
+    h = h - wall_top
+    if h < 0.5:
+        h = 0.5
+    return float(np.degrees(np.arctan2(r, h)))
+
+
+def measure_contact_angle(C, solid_mask, axis: str = "z") -> float:
+    """Contact angle estimate in degrees (lbm/fe_measure.py:85-241); the wall is
+    below the last axis ('z' in 3-D, 'y' in 2-D)."""
+    del axis  # the reference also measures along the last axis whatever it is given
+    return float(_contact_angle(_host(C), _host(solid_mask).astype(bool)))

@@ -1,0 +1,61 @@
+"""lbm.fe_measure (the package's measure_spread_factor / measure_contact_angle)
+against the reference's own lbm/fe_measure.py outputs on the same fields
+(tests/golden/fe_measure_ref.json, made by tests/golden/make_golden_measure.py):
+host path bit for bit on CPU; the device reduction of a CUDA field on the GPU
+(extents and C_max exact, the float64 volume within float32 summation error)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from make_golden_measure import HERE, inputs
+
+
+@pytest.fixture(scope="module")
+def ref():
+    with open(os.path.join(HERE, "fe_measure_ref.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("name", sorted(inputs()))
+def test_host_measurements_equal_reference(name, ref):
+    from lbm.fe_measure import measure_contact_angle, measure_spread_factor
+    phi, solid = inputs()[name]
+    r = ref[name]
+    assert measure_spread_factor(phi, solid) == r["spread"]
+    assert measure_spread_factor(phi) == r["spread_nomask"]
+    assert measure_contact_angle(phi, solid) == r["contact_angle"]
+
+
+def test_host_measurements_accept_cpu_tensors(ref):
+    torch = pytest.importorskip("torch")
+    from lbm.fe_measure import measure_contact_angle, measure_spread_factor
+    name = "cap3d_zc2.0"
+    phi, solid = inputs()[name]
+    assert measure_spread_factor(torch.from_numpy(phi), torch.from_numpy(solid)) == ref[name]["spread"]
+    assert measure_contact_angle(torch.from_numpy(phi), torch.from_numpy(solid)) == ref[name]["contact_angle"]
+
+
+def test_empty_interface():
+    from lbm.fe_measure import measure_spread_factor
+    phi = np.full((6, 5, 4), 0.25, np.float32)
+    assert measure_spread_factor(phi) == {"Dx": 0.0, "Dy": 0.0, "Dz": 0.0, "k": 0.0,
+                                          "volume": float(phi.sum()), "C_max": 0.25}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", [n for n in sorted(inputs()) if inputs()[n][0].ndim == 3])
+def test_device_spread_equals_reference(name, ref, built_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    from lbm.fe_measure import measure_spread_factor
+    phi, solid = inputs()[name]
+    for mask, key in ((torch.from_numpy(solid).cuda(), "spread"), (None, "spread_nomask")):
+        m = measure_spread_factor(torch.from_numpy(phi).cuda(), mask)
+        r = ref[name][key]
+        for k in ("Dx", "Dy", "Dz", "k", "C_max"):
+            assert m[k] == r[k], k
+        # float64 sum on the device against numpy's float32 pairwise sum
+        assert m["volume"] == pytest.approx(r["volume"], rel=2e-6 if phi.dtype == np.float32 else 1e-12)
