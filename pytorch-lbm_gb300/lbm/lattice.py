@@ -1,29 +1,48 @@
-"""D3Q19 velocity set.
+"""Lattice velocity sets: D3Q19 (the GPU path's lattice) and D2Q9.
 
-The velocity ordering, float32 weights and opposite-direction table are the
-population layout of the reference (pytorch-lbm ``lbm/lattice.py:60-96``); the
-CUDA kernels hard-code the same table (``csrc/lbm_tables.cuh``).
+The velocity ordering, float32 weights and opposite-direction tables are the
+population layout of the reference (pytorch-lbm ``lbm/lattice.py:10-96``); the
+CUDA kernels hard-code the same D3Q19 table (``csrc/lbm_common.cuh``).  D2Q9
+is provided for callers that build or inspect 2-D lattices; the GPU solver
+itself runs 3-D grids only.
 """
 import numpy as np
 import torch
 
-_E = np.array([
-    [0, 0, 0],
-    [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
-    [1, 1, 0], [-1, 1, 0], [-1, -1, 0], [1, -1, 0],
-    [1, 0, 1], [-1, 0, 1], [-1, 0, -1], [1, 0, -1],
-    [0, 1, 1], [0, -1, 1], [0, -1, -1], [0, 1, -1],
-], dtype=np.int32)
-_W = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, dtype=np.float32)
-_OPP = np.array([0, 2, 1, 4, 3, 6, 5, 9, 10, 7, 8, 13, 14, 11, 12, 17, 18, 15, 16],
-                dtype=np.int64)
+
+class Lattice:
+    """A velocity set: e (Q, dim) and w (Q,) as float32 tensors, opp (Q,) long,
+    cs2, and the derived e*w, |e|^2 and pull-streaming shifts -e."""
+
+    def __init__(self, e, w, opp, cs2=1.0 / 3.0):
+        self.dim = e.shape[1]
+        self.q = e.shape[0]
+        self.cs2 = cs2
+        self.e = torch.tensor(e, dtype=torch.float32)
+        self.w = torch.tensor(w, dtype=torch.float32)
+        self.opp = torch.tensor(opp, dtype=torch.long)
+        self.ew = self.e * self.w.unsqueeze(1)
+        self.e_sq = (self.e ** 2).sum(dim=1)
+        self.stream_shifts = -np.asarray(e, dtype=int)
 
 
-class D3Q19:
+class D2Q9(Lattice):
     def __init__(self):
-        self.dim = 3
-        self.q = 19
-        self.cs2 = 1.0 / 3.0
-        self.e = torch.tensor(_E, dtype=torch.float32)
-        self.w = torch.tensor(_W, dtype=torch.float32)
-        self.opp = torch.tensor(_OPP, dtype=torch.long)
+        e = np.array([[0, 0], [1, 0], [-1, 0], [0, 1], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1]], dtype=np.int32)
+        w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4, dtype=np.float32)
+        opp = np.array([0, 2, 1, 4, 3, 7, 8, 5, 6], dtype=np.int64)
+        super().__init__(e, w, opp)
+
+
+class D3Q19(Lattice):
+    def __init__(self):
+        e = np.array([
+            [0, 0, 0],
+            [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+            [1, 1, 0], [-1, 1, 0], [-1, -1, 0], [1, -1, 0],
+            [1, 0, 1], [-1, 0, 1], [-1, 0, -1], [1, 0, -1],
+            [0, 1, 1], [0, -1, 1], [0, -1, -1], [0, 1, -1],
+        ], dtype=np.int32)
+        w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, dtype=np.float32)
+        opp = np.array([0, 2, 1, 4, 3, 6, 5, 9, 10, 7, 8, 13, 14, 11, 12, 17, 18, 15, 16], dtype=np.int64)
+        super().__init__(e, w, opp)
