@@ -86,6 +86,30 @@ def make_case(name):
     return cfg, solid, frac, C, u
 
 
+# Solver options of the drop-in case (geometric wetting, alpha_geo = 1.5) and
+# of its variants (--mode): the reference's other interface sources and
+# wetting options on the same inputs.
+MODES = {
+    "default": dict(),
+    "cahn-hilliard": dict(interface_mode="cahn-hilliard"),
+    "mu-drive": dict(mu_drive=0.5),
+    "direct-wetting": dict(direct_wetting=True),
+    "alpha-field": dict(alpha_field=(0.5, 2.5)),
+}
+
+
+def solver_kwargs(mode, shape):
+    kw = dict(geo_amplification=1.5, geometric_wetting=True)
+    m = dict(MODES[mode])
+    if "alpha_field" in m:
+        lo, hi = m.pop("alpha_field")
+        nx, ny, nz = shape
+        ramp = np.linspace(lo, hi, nx, dtype=np.float32)[:, None, None]
+        kw["geo_amplification"] = np.ascontiguousarray(np.broadcast_to(ramp, shape))
+    kw.update(m)
+    return kw
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -222,7 +246,8 @@ def run_ours(args, rank, world, device):
 
     # --- device-resident timed region -------------------------------------
     pdt = torch.float16 if args.precision == "fp16" else torch.float32
-    s = AllenCahnSolver(cfg, dtype=pdt, geo_amplification=1.5, geometric_wetting=True)
+    skw = solver_kwargs(args.mode, (cfg.nx, cfg.ny, cfg.nz))
+    s = AllenCahnSolver(cfg, dtype=pdt, **skw)
     s.set_solid(solid, frac)
     s.init_fields(C, u)
     for _ in range(W):
@@ -269,7 +294,7 @@ def run_ours(args, rank, world, device):
     torch.cuda.synchronize(device)
     barrier(world)
     t0 = time.perf_counter()
-    s2 = AllenCahnSolver(cfg, dtype=pdt, geo_amplification=1.5, geometric_wetting=True)
+    s2 = AllenCahnSolver(cfg, dtype=pdt, **skw)
     s2.set_solid(solid, frac)
     s2.init_fields(C, u)
     reads = 0
@@ -320,6 +345,7 @@ def run_ours(args, rank, world, device):
                        "precision": ("fp16 deviation-stored populations, fp32 math and fields, fp64 global sum"
                                      if f16 else "fp32 populations, fp32 math, fp64 global sum"),
                        "parallelism": "replicas" if world > 1 else "single",
+                       "mode": args.mode,
                        "tile": list(tile), "tuned_ms": tune_ms,
                        "l2": "state (f, g: 732 MB) larger than L2 (129 MB): no flush"},
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
@@ -336,7 +362,8 @@ def run_ours(args, rank, world, device):
             "step_roofline": {"achieved_gbs": step_bw, "bytes_per_node": b_step, "peak": peak,
                               "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / b_step},
             "kernels": kernels,
-            "gpu_launches": 2 * K if two_kernel else K,
+            # two kernels per step (three with the chemical-potential pass of the grad-mu modes)
+            "gpu_launches": ((3 if args.mode in ("cahn-hilliard", "mu-drive") else 2) * K) if two_kernel else K,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "spread_after": {k2: meas[k2] for k2 in ("Dx", "Dy", "k", "z_com", "volume")},
@@ -485,6 +512,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"])
+    ap.add_argument("--mode", default="default", choices=sorted(MODES),
+                    help="solver option variant of the drop-in case (the bench line's config names it)")
     ap.add_argument("--tile", default=None, help="fixed tile 'tx,ty,tz' of the step kernel (no autotune)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -419,7 +419,10 @@ __device__ __forceinline__ T chem_pot(const Consts<T>& k, uint8_t c, T phi, T la
 // _lattice_gradient(mu_phi), lbm/fe_ac_solver.py:267-280), with the ghost
 // correction of fe_wetting.py:418-446 applied to mu itself at a boundary
 // node's solid neighbours: per direction q in order, per axis with
-// e_q != 0, grad += ((w_q e_q) mu(x + e_q)) / cs2.
+// e_q != 0, grad += (w_q e_q / cs2) mu(x + e_q).  (The reference divides each
+// term by cs2; multiplying by the folded weight differs by an ulp per term and
+// avoids 30 divisions per node: a mu_drive step on the 150x150x107 case went
+// 0.360 -> 0.304 ms.)
 template <typename T, typename St, typename MuAt, typename SolidFn>
 __device__ __forceinline__ void grad_mu(const Consts<T>& k, const St& s, int n, uint8_t c, T mu, MuAt mu_at,
                                         SolidFn nsolid, T& gx, T& gy, T& gz) {
@@ -442,10 +445,10 @@ __device__ __forceinline__ void grad_mu(const Consts<T>& k, const St& s, int n, 
       nde = __fadd_rn(nde, __fmul_rn(n2, (float)ez(q)));
       v = k.linear ? mu - (T)__fmul_rn(nde, k.h_over_kappa_f) : mu + (T)__fmul_rn(nde, k.pcok_f) * mu * (T(1) - mu);
     }
-    const T w = Lat<T>::w(q);
-    if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? w : -w, v) / Lat<T>::cs2());
-    if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? w : -w, v) / Lat<T>::cs2());
-    if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? w : -w, v) / Lat<T>::cs2());
+    const T w = Lat<T>::wc(q);
+    if (ex(q) != 0) gx = add_rn(gx, mul_rn(ex(q) > 0 ? w : -w, v));
+    if (ey(q) != 0) gy = add_rn(gy, mul_rn(ey(q) > 0 ? w : -w, v));
+    if (ez(q) != 0) gz = add_rn(gz, mul_rn(ez(q) > 0 ? w : -w, v));
   }
 }
 
@@ -1191,24 +1194,31 @@ __global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S, GMU>::blocks) k_
 
 // Grid of a persistent kernel: resident blocks per SM x SMs (one wave), at
 // most one block per kBlock nodes.  The occupancy lookup runs once per kernel
-// and device.
+// and device; host threads may launch concurrently (the serving loop sets up
+// cases on a second thread), so the cache is guarded.
 template <typename Kern>
 static cudaError_t resident_grid(Kern fn, int nodes, int* grid) {
+  static std::mutex mu;
   static int cached_dev = -1, cached = 0;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (cached_dev != dev) {
-    int nsm = 0, b = 0;
-    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, kBlock, 0);
-    if (e != cudaSuccess) return e;
-    cached = nsm * (b > 0 ? b : 1);
-    cached_dev = dev;
+  int waves;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (cached_dev != dev) {
+      int nsm = 0, b = 0;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, kBlock, 0);
+      if (e != cudaSuccess) return e;
+      cached = nsm * (b > 0 ? b : 1);
+      cached_dev = dev;
+    }
+    waves = cached;
   }
   const int full = (nodes + kBlock - 1) / kBlock;
-  *grid = cached < full ? cached : full;
+  *grid = waves < full ? waves : full;
   return cudaSuccess;
 }
 
