@@ -63,6 +63,11 @@ WORKLOADS = {
     "flat64": dict(grid=(64, 64, 48), substrate=("flat_z2",), center=(32, 32, 14), radius=12.0,
                    u=(0.0, 0.0, 0.0), theta=120.0,
                    label="flat 64x64x48 D3Q19 static droplet, theta=120, alpha_geo=1.5"),
+    # the large single solve of the precision form: convex hemisphere of radius 60 (R* = 60/45)
+    "convex384": dict(grid=(384, 384, 256), substrate=("convex", 60.0 / 45.0, 45.0), center=(192, 192, 180),
+                      radius=45.0, u=(0.0, 0.0, -0.06), theta=150.0,
+                      label="convex 384x384x256 D3Q19 droplet impact, hemisphere R=60, droplet R=45, "
+                            "theta=150, alpha_geo=1.5"),
 }
 
 
@@ -347,7 +352,8 @@ def run_ours(args, rank, world, device):
                        "parallelism": "replicas" if world > 1 else "single",
                        "mode": args.mode,
                        "tile": list(tile), "tuned_ms": tune_ms,
-                       "l2": "state (f, g: 732 MB) larger than L2 (129 MB): no flush"},
+                       "l2": f"state (f, g: {4 * 19 * n * (2 if f16 else 4) / 1e6:.0f} MB) larger than L2 "
+                             "(129 MB): no flush"},
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
                     "d2h_bytes_per_step": d2h / K,
                     "what": f"AllenCahnSolver from host arrays: create + set_solid + init_fields + {K} steps "
@@ -448,6 +454,60 @@ def run_sweep(args, device):
             "fp64_check": check}
 
 
+def run_precision(args, device):
+    """The precision form's large single solve (384x384x256 convex hemisphere,
+    droplet R = 45 at height 180, u_z = -0.06, theta = 150): the same case in
+    half-precision population storage, float32 and float64 for
+    `--precision-steps` steps each; device time per form; spread factor
+    beta = max(Dx, Dy) / (2 R), aspect k, contact angle and sum(phi) drift of
+    each form every `--precision-every` steps, and the half and float32 forms'
+    errors against the float64 run (the oracle at this size)."""
+    import torch
+    from lbm.fe_ac_solver import AllenCahnSolver
+    from lbm.fe_measure import measure_contact_angle
+    cfg, solid, frac, C, u = make_case("convex384")
+    cfg.device = str(device)
+    w = WORKLOADS["convex384"]
+    n = cfg.nx * cfg.ny * cfg.nz
+    K, every = args.precision_steps, args.precision_every
+    forms = {}
+    for name, dt in (("f16", torch.float16), ("f32", torch.float32), ("f64", torch.float64)):
+        t = time.perf_counter()
+        s = AllenCahnSolver(cfg, dtype=dt, geo_amplification=1.5, geometric_wetting=True)
+        s.set_solid(solid, frac)
+        s.init_fields(C, u)
+        setup = time.perf_counter() - t
+        m0 = s.phi_mass_init
+        hist, secs, done = [], 0.0, 0
+        while done < K:
+            k = min(every, K - done)
+            secs += _events_time(lambda: s.run(k), device)
+            done += k
+            m = s.measure()
+            ca = measure_contact_angle(s.phi, s.solid)
+            hist.append({"step": done, "beta": max(m["Dx"], m["Dy"]) / (2.0 * w["radius"]), "k": m["k"],
+                         "contact_angle": ca, "mass_drift": (m["volume"] - m0) / m0, "nan": m["has_nan"]})
+        forms[name] = {"ms_per_step": secs * 1e3 / K, "mlups": n * K / secs / 1e6, "setup_s": setup,
+                       "history": hist}
+        s.close()
+        del s
+        torch.cuda.empty_cache()
+    ref = forms["f64"]["history"][-1]
+    for name in ("f16", "f32"):
+        last = forms[name]["history"][-1]
+        forms[name]["vs_f64"] = {
+            "beta_rel_err": abs(last["beta"] - ref["beta"]) / ref["beta"] if ref["beta"] else None,
+            "k_abs_err": abs(last["k"] - ref["k"]),
+            "contact_angle_abs_err_deg": abs(last["contact_angle"] - ref["contact_angle"]),
+            "mass_drift_diff": last["mass_drift"] - ref["mass_drift"],
+            "max_beta_rel_err_over_run": max(abs(a["beta"] - b["beta"]) / b["beta"] if b["beta"] else 0.0
+                                             for a, b in zip(forms[name]["history"], forms["f64"]["history"]))}
+    return {"metric": "MLUPS", "value": forms["f16"]["mlups"], "unit": "MLUPS", "n_gpus": 1, "steps": K,
+            "higher_is_better": True, "dtype": "f16 storage / f32 math", "data": "synthetic",
+            "config": {"workload": w["label"] + f", {K} steps", "nodes": n},
+            "forms": forms, "speedup_f16_vs_f32": forms["f16"]["mlups"] / forms["f32"]["mlups"]}
+
+
 def run_serve(args, device):
     """The serving loop: `--serve-requests` impact requests (grids up to
     256x256x192, steps U[1000, 4000]) with Poisson arrivals (4 per second),
@@ -500,11 +560,13 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)  # the drop-in case's own step count
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ridge150", choices=sorted(WORKLOADS) + ["serve", "sweep"])
+    ap.add_argument("--workload", default="ridge150", choices=sorted(WORKLOADS) + ["serve", "sweep", "precision"])
     ap.add_argument("--seed", type=int, default=0, help="first seed of the sweep / serving cases")
     ap.add_argument("--sweep-cases", type=int, default=64)
     ap.add_argument("--sweep-steps", type=int, default=1500)
     ap.add_argument("--sweep-check", type=int, default=4, help="sweep cases also run in float64")
+    ap.add_argument("--precision-steps", type=int, default=5000, help="steps of the precision-form solve")
+    ap.add_argument("--precision-every", type=int, default=500, help="measurement interval of that solve")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--cpu-steps", type=int, default=3)
@@ -528,10 +590,11 @@ def main():
     import torch
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
-    if args.workload in ("sweep", "serve"):
+    if args.workload in ("sweep", "serve", "precision"):
         if world > 1:
-            raise SystemExit("the sweep and serving workloads run on one GPU")
-        out = run_sweep(args, device) if args.workload == "sweep" else run_serve(args, device)
+            raise SystemExit("the sweep, serving and precision workloads run on one GPU")
+        run = {"sweep": run_sweep, "serve": run_serve, "precision": run_precision}[args.workload]
+        out = run(args, device)
         print(json.dumps(out), flush=True)
         return
     if world > 1:
