@@ -282,8 +282,10 @@ int lbm_load_state(LbmHandle* h, const void* host, int64_t bytes, void* stream);
 int lbm_status(LbmHandle* h, uint32_t* flags);
 
 /* Bytes of device memory lbm_create allocates for an nx*ny*nz grid of the
- * given precision (the admission size of a case).  No GPU needed.  No
- * reference counterpart. */
+ * given precision (the admission size of a case).  The gradient-of-mu modes
+ * (Cahn-Hilliard, mu_drive) add 4 arrays of the padded node count in the
+ * compute type, a per-node amplification field one of N elements.  No GPU
+ * needed.  No reference counterpart. */
 int lbm_footprint(int64_t nx, int64_t ny, int64_t nz, int precision, int64_t* bytes);
 
 /*

@@ -92,6 +92,7 @@ struct LbmHandle {
   void* meas_phi = nullptr;      // N x T scratch for lbm_measure
   void* amp = nullptr;           // N x T per-node geometric amplification (lbm_set_amplification), or null
   void* mu = nullptr;            // Np x T chemical potential of the step (gradient-of-mu modes only)
+  void* gmu = nullptr;           // 3 Np x T its gradient (gradient-of-mu modes only)
   int* nsw = nullptr;            // N next-interior node indices (direct wetting only)
   void* cubic = nullptr;         // 4 x T cubic-wall-energy constants (direct wetting only)
   // derived
@@ -276,6 +277,7 @@ State<T, S> make_state(const LbmHandle& h, int in_buf, int phi_in) {
   s.eps = static_cast<const T*>(h.eps);
   s.amp = static_cast<const T*>(h.amp);
   s.mu = static_cast<T*>(h.mu);
+  s.gmu = static_cast<T*>(h.gmu);
   s.nsw = h.nsw;
   s.cubic = static_cast<const T*>(h.cubic);
   s.partials = h.partials;
@@ -332,7 +334,7 @@ Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz, i
 void free_all(LbmHandle* h) {
   void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u,        h->phi[0], h->phi[1], h->eps,
                   h->cls,  h->wn,   h->partials, h->counters, h->cbuf, h->scal, h->meas_phi, h->desc,
-                  h->amp,  h->mu, h->nsw, h->cubic};
+                  h->amp,  h->mu, h->gmu, h->nsw, h->cubic};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -552,7 +554,10 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   A(&h->cbuf, z.cbuf);
   A((void**)&h->scal, z.scal);
   A(&h->meas_phi, z.meas_phi);
-  if (gmu) A(&h->mu, z.phi);
+  if (gmu) {
+    A(&h->mu, z.phi);
+    A(&h->gmu, 3 * z.phi);
+  }
   if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(h->phi[0], 0, Np * T);
   if (e == cudaSuccess) e = cudaMemset(h->phi[1], 0, Np * T);

@@ -187,7 +187,8 @@ struct State {
   const float* wn;  // wall normal [3][N] (non-zero at boundary nodes only)
   const T* eps;     // solid fraction (read at partial nodes only)
   const T* amp;     // per-node geometric amplification (read at boundary nodes only; null: the scalar k.amp)
-  T* mu;            // chemical potential of this step [N] (k_mu; the gradient-of-mu modes only)
+  T* mu;            // chemical potential of this step [Np] (k_mu; the gradient-of-mu modes only)
+  T* gmu;           // its isotropic gradient [3][Np] (k_gradmu; the gradient-of-mu modes only)
   const int* nsw;   // next-interior fluid node of a boundary node or -1 [N] (direct wetting only)
   // direct wetting (cubic wall energy, fe_wetting.py:369-416), null when off:
   // (1 - a)^2, 4 a, -(1 - a), 2 a with a = 6 sigma cos(theta) / kappa (2 a = 0: no cubic root).

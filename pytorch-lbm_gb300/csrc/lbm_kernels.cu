@@ -421,8 +421,7 @@ __device__ __forceinline__ T chem_pot(const Consts<T>& k, uint8_t c, T phi, T la
 // node's solid neighbours: per direction q in order, per axis with
 // e_q != 0, grad += (w_q e_q / cs2) mu(x + e_q).  (The reference divides each
 // term by cs2; multiplying by the folded weight differs by an ulp per term and
-// avoids 30 divisions per node: a mu_drive step on the 150x150x107 case went
-// 0.360 -> 0.304 ms.)
+// avoids 30 divisions per node.)
 template <typename T, typename St, typename MuAt, typename SolidFn>
 __device__ __forceinline__ void grad_mu(const Consts<T>& k, const St& s, int n, uint8_t c, T mu, MuAt mu_at,
                                         SolidFn nsolid, T& gx, T& gy, T& gz) {
@@ -663,9 +662,9 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     T cl = L.cs2() * lam * k.ac_scale * rcp(gm);
     if (k.wetting) cl = cl * (T(1) - k.sharpen_reduce * k.ww[c >> kWwShift]);
     if constexpr (GMU) {
-      T mx, my, mz;
-      grad_mu(k, s, n, c, mu, [&](int q) { return ld_pol(s.mu + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); },
-              solid_at, mx, my, mz);
+      // grad mu of this node (k_gradmu)
+      const T mx = ld_pol(s.gmu + nu, pol.once), my = ld_pol(s.gmu + (Nu + nu), pol.once),
+              mz = ld_pol(s.gmu + (2 * Nu + nu), pol.once);
       if (k.gmu_mode == kGmuCH) {
         // Cahn-Hilliard: d(phi u) + M (grad mu - grad phi) tau_f / (tau_f - 1/2)  (:457-461)
         S0 = d0 + (k.mob * (mx - gx)) * k.guo;
@@ -1080,7 +1079,7 @@ __global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
 // 150x150x107 case 141 -> 127 us per update launch against 3 blocks without spills.
 template <typename T, typename S, bool GMU = false>
 struct UpdateOccupancy {
-  static constexpr int blocks = sizeof(T) == 8 ? 1 : (GMU ? 3 : 4);
+  static constexpr int blocks = sizeof(T) == 8 ? 1 : 4;
 };
 
 template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool GMU>
@@ -1106,6 +1105,27 @@ template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool GMU = 
 __global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S, GMU>::blocks) k_update(Consts<T> k, State<T, S> s) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
   if (n < k.N) update_one<T, S, RAW, FIRST, OMEGA1, GMU>(k, s, n, Pol::make());
+}
+
+// Gradient of the chemical potential of every node (mu from k_mu), for the
+// modes whose interface source needs it; read by the update kernel.
+template <typename T, typename S>
+__global__ void __launch_bounds__(kBlock) k_gradmu(Consts<T> k, State<T, S> s) {
+  const int n = blockIdx.x * kBlock + threadIdx.x;
+  if (n >= k.N) return;
+  int ix, iy, iz;
+  decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
+  const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
+  const Pol pol = Pol::make();
+  const uint8_t c = s.cls[n];
+  const T mu = ld_pol(s.mu + n, pol.keep);
+  T mx, my, mz;
+  grad_mu(k, s, n, c, mu, [&](int q) { return ld_pol(s.mu + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); },
+          [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; }, mx, my, mz);
+  const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+  st_pol(s.gmu + nu, mx, pol.keep);
+  st_pol(s.gmu + (Nu + nu), my, pol.keep);
+  st_pol(s.gmu + (2 * Nu + nu), mz, pol.keep);
 }
 
 // Chemical potential of every node of this step (phi from the phi kernel),
@@ -1569,6 +1589,7 @@ static cudaError_t launch_two_t(const Consts<T>& k, const State<T, S>& s, cudaSt
     // (later steps run the batched kernels)
     if constexpr (RAW && FIRST && sizeof(S) != 2) {
       k_mu<T, S><<<blocks, kBlock, 0, st>>>(k, s);
+      k_gradmu<T, S><<<blocks, kBlock, 0, st>>>(k, s);
       k_update<T, S, RAW, FIRST, OMEGA1, true><<<blocks, kBlock, 0, st>>>(k, s);
       return cudaGetLastError();
     } else {
@@ -1648,11 +1669,13 @@ cudaError_t launch_update_batch(const void* cases, const unsigned short* b2c, in
   if (omega1) return launch_pdl(k_update_batch<T, S, true>, blocks, st, c, b2c);
   return launch_pdl(k_update_batch<T, S, false>, blocks, st, c, b2c);
 }
-// k_mu of one grid (plain stream order: it waits for the phi kernel, and the
+// k_mu and k_gradmu of one grid (plain stream order: they wait for the phi kernel, and the
 // next update kernel waits for it).
 template <typename T, typename S>
 cudaError_t launch_mu(const Consts<T>& k, const State<T, S>& s, cudaStream_t st) {
-  k_mu<T, S><<<(k.N + kBlock - 1) / kBlock, kBlock, 0, st>>>(k, s);
+  const int blocks = (k.N + kBlock - 1) / kBlock;
+  k_mu<T, S><<<blocks, kBlock, 0, st>>>(k, s);
+  k_gradmu<T, S><<<blocks, kBlock, 0, st>>>(k, s);
   return cudaGetLastError();
 }
 template <typename T, typename S>
