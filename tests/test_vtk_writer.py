@@ -37,3 +37,17 @@ def test_vtk_torch_inputs(tmp_path, built_lib):
     write_vtk(str(b), torch.from_numpy(rho), torch.from_numpy(u), solid=torch.from_numpy(solid), dx=dx,
               step=step, t=t)
     assert a.read_bytes() == b.read_bytes()
+
+
+def test_vtk_unwritable_path_raises(tmp_path, built_lib):
+    from io_utils import write_vtk
+    rho, u, solid, dx, step, t = vtk_cases()["f32_3d"]
+    blocker = tmp_path / "file"
+    blocker.write_text("x")
+    with pytest.raises(OSError):
+        write_vtk(str(blocker / "sub" / "a.vtk"), rho, u)  # a directory under a regular file
+
+
+def test_native_vtk_rejects_null_arguments(tmp_path, built_lib):
+    lib = built_lib
+    assert lib.lbm_write_vtk(str(tmp_path / "a.vtk").encode(), b"", 1, None, None, None, None, None) == -1
