@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "lbm_tables.h"
@@ -24,6 +25,24 @@ inline int64_t idx(int64_t ix, int64_t iy, int64_t iz, int64_t ny, int64_t nz) {
 }
 
 inline int64_t wrap(int64_t i, int64_t n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// fn(begin, end) over [0, n) split into contiguous ranges on the host's
+// cores.  Every loop it runs computes each index independently, so the
+// result does not depend on the split.
+template <typename Fn>
+void parallel_for(int64_t n, Fn fn) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  int64_t nt = std::min<int64_t>(hw ? hw : 1, 32);
+  if (n < 4096 || nt < 2) {
+    fn((int64_t)0, n);
+    return;
+  }
+  nt = std::min<int64_t>(nt, n);
+  std::vector<std::thread> th;
+  for (int64_t t = 1; t < nt; ++t) th.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+  fn((int64_t)0, n / nt);
+  for (auto& x : th) x.join();
+}
 
 // Smooth wall normals -grad(frac)/|grad(frac)| at boundary nodes, with
 // np.gradient's stencil (central inside, one-sided first order at the edges)
@@ -43,7 +62,8 @@ void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, 
     if (i == n_ax - 1) return (F)(at(n_ax - 1) - at(n_ax - 2)) / (F)1.0;
     return (F)(at(i + 1) - at(i - 1)) / (F)2.0;
   };
-  for (int64_t ix = 0; ix < nx; ++ix)
+  parallel_for(nx, [&](int64_t x0, int64_t x1) {
+  for (int64_t ix = x0; ix < x1; ++ix)
     for (int64_t iy = 0; iy < ny; ++iy)
       for (int64_t iz = 0; iz < nz; ++iz) {
         const int64_t n = idx(ix, iy, iz, ny, nz);
@@ -61,6 +81,7 @@ void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, 
         wn[N + n] = (float)((-g1) / mag);
         wn[2 * N + n] = (float)((-g2) / mag);
       }
+  });
 }
 
 }  // namespace
@@ -97,21 +118,19 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
   g.n_boundary = 0;
 
   if (wetting) {
-    // boundary: fluid node whose periodic neighbour x - e_q is solid for some q
+    // boundary: fluid node whose periodic neighbour x - e_q is solid for some
+    // q, found from the solid side: every fluid x = m + e_q of a solid m
+    // (solid nodes are the smaller set)
     for (int64_t ix = 0; ix < nx; ++ix)
       for (int64_t iy = 0; iy < ny; ++iy)
         for (int64_t iz = 0; iz < nz; ++iz) {
-          const int64_t n = idx(ix, iy, iz, ny, nz);
-          if (g.solid[n]) continue;
+          if (!g.solid[idx(ix, iy, iz, ny, nz)]) continue;
           for (int q = 1; q < kQ; ++q) {
-            const int64_t m = idx(wrap(ix - kE[q][0], nx), wrap(iy - kE[q][1], ny), wrap(iz - kE[q][2], nz), ny, nz);
-            if (g.solid[m]) {
-              g.boundary[n] = 1;
-              ++g.n_boundary;
-              break;
-            }
+            const int64_t n = idx(wrap(ix + kE[q][0], nx), wrap(iy + kE[q][1], ny), wrap(iz + kE[q][2], nz), ny, nz);
+            if (!g.solid[n]) g.boundary[n] = 1;
           }
         }
+    for (int64_t n = 0; n < N; ++n) g.n_boundary += g.boundary[n];
     // wall normals
     if (fraction_dtype == 1) {
       smooth_normals(static_cast<const float*>(fraction), g.boundary, nx, ny, nz, g.wall_normal);
