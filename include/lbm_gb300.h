@@ -226,6 +226,15 @@ int lbm_get_scalars(LbmHandle* h, double* phi_mass_init, double* last_sum_phi,
  * scripts/run_thesis_sweep.py:182-216. */
 int lbm_measure(LbmHandle* h, double* out9, void* stream);
 
+/* Global reductions of the current fields on the device, in float64: sum of
+ * phi (solid nodes zeroed), total momentum sum rho(phi) u with rho = phi rho_l
+ * + (1 - phi) rho_g, the first and last x, y, z index of the phi > 0.5 set
+ * (extents6 = xmin, xmax, ymin, ymax, zmin, zmax; all -1 when the set is
+ * empty) and the maximum of phi.  Host outputs (any may be NULL); synchronises
+ * `stream`.  The mass/momentum guard of a solve and the data behind
+ * measure_spread_factor (lbm/fe_measure.py:11-82). */
+int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, float* cmax, void* stream);
+
 /* Maximum node count of lbm_measure_static (its indexing is 32-bit). */
 #define LBM_MEASURE_STATIC_MAX_NODES (1LL << 30)
 

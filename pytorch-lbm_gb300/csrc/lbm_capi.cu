@@ -34,7 +34,10 @@ cudaError_t launch_inject(const Consts<T>&, const State<T, S>&, bool, const Inje
                           cudaStream_t);
 template <typename T>
 cudaError_t launch_measure(int, int, int, const T*, const uint8_t*, double*, int, unsigned*, double*,
-                           cudaStream_t);
+                           cudaStream_t, double* = nullptr);
+template <typename T>
+cudaError_t launch_momentum(int, const T*, const T*, int, double, double, double*, int, unsigned*, double*,
+                            cudaStream_t);
 template <typename T>
 cudaError_t launch_measure_static(int, int, int, const T*, const uint8_t*, double*, cudaStream_t);
 template <typename T, typename S>
@@ -86,9 +89,9 @@ struct LbmHandle {
   uint8_t* cls = nullptr;
   float* wn = nullptr;
   double* partials = nullptr;
-  unsigned* counters = nullptr;  // [0] step/init reductions, [1] measure, [2] status
+  unsigned* counters = nullptr;  // [0] step/init reductions, [1] measure, [2] status, [3] inject, [4] momentum
   void* cbuf = nullptr;          // 2 x T
-  double* scal = nullptr;        // [0] phi_mass_init [1] last sum [2..10] measure output
+  double* scal = nullptr;        // [0] phi_mass_init [1] last sum [2..10] measure output [16..21] extents [24..26] momentum
   void* meas_phi = nullptr;      // N x T scratch for lbm_measure
   void* amp = nullptr;           // N x T per-node geometric amplification (lbm_set_amplification), or null
   void* mu = nullptr;            // Np x T chemical potential of the step (gradient-of-mu modes only)
@@ -478,9 +481,9 @@ Sizes sizes_of(int64_t nx, int64_t ny, int64_t nz, int precision) {
   z.cls = Np;
   z.wn = 3 * N * sizeof(float);
   z.partials = npart * sizeof(double);
-  z.counters = 4 * sizeof(unsigned);
+  z.counters = 8 * sizeof(unsigned);
   z.cbuf = 2 * T;
-  z.scal = 16 * sizeof(double);
+  z.scal = 32 * sizeof(double);
   z.meas_phi = N * T;
   return z;
 }
@@ -558,11 +561,11 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
     A(&h->mu, z.phi);
     A(&h->gmu, 3 * z.phi);
   }
-  if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 8 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(h->phi[0], 0, Np * T);
   if (e == cudaSuccess) e = cudaMemset(h->phi[1], 0, Np * T);
   if (e == cudaSuccess) e = cudaMemset(h->cls, 0, Np);
-  if (e == cudaSuccess) e = cudaMemset(h->scal, 0, 16 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(h->scal, 0, 32 * sizeof(double));
   if (e != cudaSuccess) {
     free_all(h);
     delete h;
@@ -1126,6 +1129,40 @@ int lbm_load_state(LbmHandle* h, const void* host, int64_t bytes, void* stream) 
   h->steps = hd.steps;
   h->initialized = true;
   h->desc_ok = false;
+  return LBM_OK;
+}
+
+int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, float* cmax, void* stream) {
+  if (!h) return fail(LBM_E_ARG, "lbm_reduce: null handle");
+  if (!h->initialized) return fail(LBM_E_STATE, "lbm_reduce: not initialised");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = lbm_get_fields(h, LBM_FIELD_PHI, h->meas_phi, nullptr, nullptr, nullptr, nullptr, nullptr, stream);
+  if (rc) return rc;
+  const int nx = (int)h->nx, ny = (int)h->ny, nz = (int)h->nz, N = (int)h->N, us = (int)h->Np;
+  cudaError_t e;
+  if (h->prec != LBM_F64) {
+    e = launch_measure<float>(nx, ny, nz, (const float*)h->meas_phi, h->cls, h->partials, kMeasureBlocks,
+                              h->counters + 1, h->scal + 2, st, h->scal + 16);
+    if (e == cudaSuccess)
+      e = launch_momentum<float>(N, (const float*)h->meas_phi, (const float*)h->u, us, h->prm.rho_l, h->prm.rho_g,
+                                 h->partials, kMeasureBlocks, h->counters + 4, h->scal + 24, st);
+  } else {
+    e = launch_measure<double>(nx, ny, nz, (const double*)h->meas_phi, h->cls, h->partials, kMeasureBlocks,
+                               h->counters + 1, h->scal + 2, st, h->scal + 16);
+    if (e == cudaSuccess)
+      e = launch_momentum<double>(N, (const double*)h->meas_phi, (const double*)h->u, us, h->prm.rho_l,
+                                  h->prm.rho_g, h->partials, kMeasureBlocks, h->counters + 4, h->scal + 24, st);
+  }
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_reduce: ") + cudaGetErrorString(e));
+  double r[25];
+  CUDA_TRY(cudaMemcpyAsync(r, h->scal + 2, sizeof(r), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (sum_phi) *sum_phi = r[0];
+  if (cmax) *cmax = (float)r[1];
+  if (extents6)
+    for (int j = 0; j < 6; ++j) extents6[j] = (int32_t)r[14 + j];
+  if (mom3)
+    for (int d = 0; d < 3; ++d) mom3[d] = r[22 + d];
   return LBM_OK;
 }
 

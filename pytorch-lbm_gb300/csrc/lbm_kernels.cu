@@ -1478,7 +1478,7 @@ __device__ __forceinline__ void meas_merge(A& r, const B& q) {
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, const T* __restrict__ phi,
                                                    const uint8_t* __restrict__ cls, double* partials,
-                                                   unsigned* counter, double* out) {
+                                                   unsigned* counter, double* out, double* ext6) {
   const int N = nx * ny * nz;
   double v[kMeasVals] = {0.0, -1e300, 1e300, -1e300, 1e300, -1e300, 1e300, -1e300, 0.0, 0.0, 0.0};
   for (int n = blockIdx.x * kBlock + threadIdx.x; n < N; n += gridDim.x * kBlock) {
@@ -1554,8 +1554,60 @@ __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, cons
     out[6] = any ? r[8] / r[9] : 0.0;
     out[7] = r[9];
     out[8] = r[10];
+    if (ext6) {
+      // first and last index of the phi > 0.5 set along x, y, z (-1 when empty)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) ext6[j] = any ? r[2 + j] : -1.0;
+    }
     *counter = 0u;
   }
+}
+
+// Total momentum sum_x rho(phi) u of a field pair (phi dense [N], u with
+// component stride us), rho = phi rho_l + (1 - phi) rho_g, accumulated in
+// float64 per node in a fixed order (block partials, then the last block
+// sums them in block order).  Writes out3.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_momentum(int N, const T* __restrict__ phi, const T* __restrict__ u,
+                                                    int us, double rho_l, double rho_g, double* partials,
+                                                    unsigned* counter, double* out3) {
+  double m[3] = {0.0, 0.0, 0.0};
+  for (int n = blockIdx.x * kBlock + threadIdx.x; n < N; n += gridDim.x * kBlock) {
+    const double p = (double)phi[n];
+    const double rho = p * rho_l + (1.0 - p) * rho_g;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) m[d] += rho * (double)u[(size_t)d * us + n];
+  }
+  __shared__ double sw[kBlock / 32][3];
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double v = m[d];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sw[wid][d] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int d = 0; d < 3; ++d) {
+      double v = 0.0;
+      for (int w = 0; w < kBlock / 32; ++w) v += sw[w][d];
+      partials[(size_t)blockIdx.x * 3 + d] = v;
+    }
+    __threadfence();
+    s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  const volatile double* pp = partials;
+  for (int d = 0; d < 3; ++d) {
+    double v = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) v += pp[(size_t)b * 3 + d];
+    out3[d] = v;
+  }
+  *counter = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -1734,13 +1786,25 @@ cudaError_t launch_populations(const Consts<T>& k, const State<T, S>& s, bool ra
 
 template <typename T>
 cudaError_t launch_measure(int nx, int ny, int nz, const T* phi, const uint8_t* cls, double* partials,
-                           int max_blocks, unsigned* counter, double* out, cudaStream_t st) {
+                           int max_blocks, unsigned* counter, double* out, cudaStream_t st, double* ext6) {
   const int N = nx * ny * nz;
   int grid = (N + kBlock - 1) / kBlock;
   if (grid > max_blocks) grid = max_blocks;
-  k_measure<T><<<grid, kBlock, 0, st>>>(nx, ny, nz, phi, cls, partials, counter, out);
+  k_measure<T><<<grid, kBlock, 0, st>>>(nx, ny, nz, phi, cls, partials, counter, out, ext6);
   return cudaGetLastError();
 }
+template <typename T>
+cudaError_t launch_momentum(int N, const T* phi, const T* u, int us, double rho_l, double rho_g, double* partials,
+                            int max_blocks, unsigned* counter, double* out3, cudaStream_t st) {
+  int grid = (N + kBlock - 1) / kBlock;
+  if (grid > max_blocks) grid = max_blocks;
+  k_momentum<T><<<grid, kBlock, 0, st>>>(N, phi, u, us, rho_l, rho_g, partials, counter, out3);
+  return cudaGetLastError();
+}
+template cudaError_t launch_momentum<float>(int, const float*, const float*, int, double, double, double*, int,
+                                            unsigned*, double*, cudaStream_t);
+template cudaError_t launch_momentum<double>(int, const double*, const double*, int, double, double, double*, int,
+                                             unsigned*, double*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Allocation-free spread diagnostics.  Some callers cannot allocate device
@@ -1802,7 +1866,7 @@ cudaError_t launch_measure_static(int nx, int ny, int nz, const T* phi, const ui
   // the counter must start at zero: a launch that failed part-way leaves it set
   e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
-  return launch_measure<T>(nx, ny, nz, phi, solid, partials, kStaticMeasBlocks, counter, out, st);
+  return launch_measure<T>(nx, ny, nz, phi, solid, partials, kStaticMeasBlocks, counter, out, st, nullptr);
 }
 template cudaError_t launch_measure_static<float>(int, int, int, const float*, const uint8_t*, double*, cudaStream_t);
 template cudaError_t launch_measure_static<double>(int, int, int, const double*, const uint8_t*, double*,
@@ -1842,7 +1906,9 @@ LBM_INSTANTIATE_BATCH(double, double)
 LBM_INSTANTIATE_BATCH(float, __half)
 #undef LBM_INSTANTIATE_BATCH
 
-template cudaError_t launch_measure<float>(int, int, int, const float*, const uint8_t*, double*, int, unsigned*, double*, cudaStream_t);
-template cudaError_t launch_measure<double>(int, int, int, const double*, const uint8_t*, double*, int, unsigned*, double*, cudaStream_t);
+template cudaError_t launch_measure<float>(int, int, int, const float*, const uint8_t*, double*, int, unsigned*,
+                                           double*, cudaStream_t, double*);
+template cudaError_t launch_measure<double>(int, int, int, const double*, const uint8_t*, double*, int, unsigned*,
+                                            double*, cudaStream_t, double*);
 
 }  // namespace lbm

@@ -27,7 +27,7 @@ EXPORTS = (
     "lbm_set_tile", "lbm_get_tile", "lbm_autotune", "lbm_measure_static", "lbm_footprint",
     "lbm_batch_create", "lbm_batch_step", "lbm_batch_size", "lbm_batch_autotune", "lbm_batch_destroy",
     "lbm_inject_droplet", "lbm_set_amplification", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
-    "lbm_write_vtk",
+    "lbm_write_vtk", "lbm_reduce",
 )
 
 
@@ -81,6 +81,8 @@ def _declare(L):
         "lbm_save_state": ([_vp, _vp, _i64, _vp], _i32),
         "lbm_load_state": ([_vp, _vp, _i64, _vp], _i32),
         "lbm_write_vtk": ([ctypes.c_char_p, ctypes.c_char_p, _i64, _vp, _vp, _vp, _vp, _vp], _i32),
+        "lbm_reduce": ([_vp, ctypes.POINTER(_dbl), ctypes.POINTER(_dbl), ctypes.POINTER(ctypes.c_int32),
+                        ctypes.POINTER(ctypes.c_float), _vp], _i32),
         "lbm_status": ([_vp, ctypes.POINTER(_u32)], _i32),
         "lbm_set_tile": ([_vp, _i32, _i32, _i32], _i32),
         "lbm_get_tile": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),

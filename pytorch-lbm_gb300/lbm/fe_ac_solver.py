@@ -403,6 +403,17 @@ class AllenCahnSolver:
         d["has_nan"] = bool(d["has_nan"])
         return d
 
+    def reduce(self, stream=None):
+        """Global float64 reductions of the current fields on the device:
+        sum_phi, momentum (sum rho u, 3 components), extents (first and last
+        x, y, z index of phi > 0.5; -1 when empty), C_max."""
+        sp, cm = ctypes.c_double(), ctypes.c_float()
+        mom = (ctypes.c_double * 3)()
+        ext = (ctypes.c_int32 * 6)()
+        nat.check(self._lib.lbm_reduce(self._h, ctypes.byref(sp), mom, ext, ctypes.byref(cm),
+                                       nat.stream_ptr(stream)), "lbm_reduce")
+        return {"sum_phi": sp.value, "momentum": tuple(mom), "extents": tuple(ext), "C_max": cm.value}
+
     def autotune(self, reps=5, stream=None):
         """Pick the fastest step kernel (the two-kernel step or a tile shape of
         the fused kernel) on the current state (the state is left unchanged).

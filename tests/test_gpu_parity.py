@@ -223,3 +223,31 @@ def test_inject_droplet_vs_reference_and_oracle(dn):
         o.step()
     assert np.abs(_np(s.phi) - gd["after_phi"]).max() <= (2e-4 if dn == "float32" else 1e-9)
     assert rel_l2(_np(s.u), gd["after_u"]) <= (1e-3 if dn == "float32" else 1e-8)
+
+
+@pytest.mark.parametrize("dn", ["float32", "float64"])
+def test_reduce_matches_fields(dn):
+    """lbm_reduce (sum of phi, momentum sum rho u, phi > 0.5 extents, C_max in
+    float64 on the device) against the same sums over the fields on the host."""
+    case, s = _gpu("ridge_l162", dn)
+    s.run(6)
+    r = s.reduce()
+    phi, vel = _np(s.phi).astype(np.float64), _np(s.u).astype(np.float64)
+    solid = _np(s.solid)
+    phi_c = np.where(solid, 0.0, phi)
+    cfg = s.config
+    rho = phi * cfg.rho_l + (1.0 - phi) * cfg.rho_g
+    mom = (rho[None] * vel).reshape(3, -1).sum(axis=1)
+    scale = np.abs(rho[None] * vel).reshape(3, -1).sum(axis=1)
+    assert r["sum_phi"] == pytest.approx(phi_c.sum(), rel=1e-12)
+    assert np.all(np.abs(np.array(r["momentum"]) - mom) <= 1e-10 * scale + 1e-300)
+    idx = np.argwhere(phi_c > 0.5)
+    ext = []
+    for d in range(3):
+        ext += [int(idx[:, d].min()), int(idx[:, d].max())]
+    assert r["extents"] == tuple(ext)
+    assert r["C_max"] == pytest.approx(float(phi_c.max()), rel=1e-7)
+    # an empty phi > 0.5 set reports -1 extents
+    case2, e = _gpu("flat_q120", dn)
+    e.init_fields(np.full(e.shape, 0.25, np.float32))
+    assert e.reduce()["extents"] == (-1,) * 6
