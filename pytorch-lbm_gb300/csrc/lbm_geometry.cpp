@@ -44,9 +44,11 @@ void parallel_for(int64_t n, Fn fn) {
   for (auto& x : th) x.join();
 }
 
-// Smooth wall normals -grad(frac)/|grad(frac)| at boundary nodes, with
+// Smooth wall normals -grad(frac)/|grad(frac)| times the boundary mask, with
 // np.gradient's stencil (central inside, one-sided first order at the edges)
-// evaluated in the fraction's own type F (fe_wetting.py:242-267).
+// evaluated in the fraction's own type F (fe_wetting.py:242-267).  Every node
+// is computed: off the boundary the product with the mask is a signed zero
+// (-0 where -grad/|grad| is negative or -0), as in the reference's array.
 template <typename F>
 void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, int64_t ny, int64_t nz,
                     std::vector<float>& wn) {
@@ -67,7 +69,7 @@ void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, 
     for (int64_t iy = 0; iy < ny; ++iy)
       for (int64_t iz = 0; iz < nz; ++iz) {
         const int64_t n = idx(ix, iy, iz, ny, nz);
-        if (!bnd[n]) continue;
+        const F mask = bnd[n] ? (F)1 : (F)0;
         const F g0 = grad_axis(ix, iy, iz, 0);
         const F g1 = grad_axis(ix, iy, iz, 1);
         const F g2 = grad_axis(ix, iy, iz, 2);
@@ -77,9 +79,9 @@ void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, 
         acc = acc + g2 * g2;
         F mag = std::sqrt(acc);
         if (mag < (F)1e-10) mag = (F)1e-10;
-        wn[n] = (float)((-g0) / mag);
-        wn[N + n] = (float)((-g1) / mag);
-        wn[2 * N + n] = (float)((-g2) / mag);
+        wn[n] = (float)(((-g0) / mag) * mask);
+        wn[N + n] = (float)(((-g1) / mag) * mask);
+        wn[2 * N + n] = (float)(((-g2) / mag) * mask);
       }
   });
 }

@@ -62,8 +62,9 @@ def test_native_geometry_bit_exact(built_lib, name, dn):
     assert np.array_equal(o["cls"] & 1 == 1, gd["solid"])
     if "is_boundary" in gd:
         assert np.array_equal(o["bnd"], gd["is_boundary"])
-        assert np.array_equal(o["wn"], gd["wall_normal"])
-        assert np.array_equal(o["ww"], gd["wall_weight"])
+        # bit for bit, signed zeros included
+        assert np.array_equal(o["wn"].view(np.uint32), gd["wall_normal"].view(np.uint32))
+        assert np.array_equal(o["ww"].view(np.uint32), gd["wall_weight"].view(np.uint32))
         assert np.array_equal(o["near"], gd["near_wall"])
     else:
         assert not o["bnd"].any()
