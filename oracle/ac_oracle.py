@@ -47,7 +47,16 @@ W32 = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, dtype=np.float32)
 OPP = np.array([0, 2, 1, 4, 3, 6, 5, 9, 10, 7, 8, 13, 14, 11, 12, 17, 18, 15, 16],
                dtype=np.int64)
 Q = 19
+# D2Q9 tables of the 2-D (nz == 1) grids, lbm/lattice.py:36-57.
+E2 = np.array([[0, 0], [1, 0], [-1, 0], [0, 1], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1]], dtype=np.int64)
+W2_32 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4, dtype=np.float32)
+OPP2 = np.array([0, 2, 1, 4, 3, 7, 8, 5, 6], dtype=np.int64)
 CS2 = 1.0 / 3.0
+
+
+def lattice_tables(ndim):
+    """(e, float32 w, opp, q) of D2Q9 for ndim == 2, D3Q19 for ndim == 3."""
+    return (E2, W2_32, OPP2, 9) if ndim == 2 else (E, W32, OPP, Q)
 XI_NEAR_WALL = 5.0  # hard-coded interface width of the near-wall weight (lbm/fe_wetting.py:81)
 
 
@@ -61,12 +70,12 @@ def _seqsum(a):
 
 def _shift_from(a, e):
     """Return b with b[x] = a[x + e] (periodic) == torch.roll(a, -e)."""
-    return np.roll(a, shift=(-int(e[0]), -int(e[1]), -int(e[2])), axis=(0, 1, 2))
+    return np.roll(a, shift=tuple(-int(x) for x in e), axis=tuple(range(len(e))))
 
 
 def _shift_to(a, e):
     """Return b with b[x] = a[x - e] (periodic) == torch.roll(a, +e)."""
-    return np.roll(a, shift=(int(e[0]), int(e[1]), int(e[2])), axis=(0, 1, 2))
+    return np.roll(a, shift=tuple(int(x) for x in e), axis=tuple(range(len(e))))
 
 
 def _exp_f32(x):
@@ -110,37 +119,42 @@ class OracleWetting:
     def _precompute(self, frac):
         solid = self.solid
         shape = solid.shape
+        D = solid.ndim
+        E_, _, _, Q_ = lattice_tables(D)
+        self.E, self.Q = E_, Q_
         # is_boundary: fluid node with a solid neighbour, periodic (fe_wetting.py:129-140)
         isb = np.zeros(shape, dtype=bool)
-        for i in range(1, Q):
-            isb |= _shift_to(solid, E[i]) & ~solid
+        for i in range(1, Q_):
+            isb |= _shift_to(solid, E_[i]) & ~solid
         self.is_boundary = isb
 
-        wn = np.zeros((3,) + shape, dtype=np.float32)
+        wn = np.zeros((D,) + shape, dtype=np.float32)
         if frac is not None:
             # smooth normals: -grad(frac)/|grad(frac)| in frac's dtype (fe_wetting.py:242-267)
             grad = np.gradient(frac)
             mag = np.sqrt(sum(gd ** 2 for gd in grad))
             mag[mag < 1e-10] = 1e-10
-            for d in range(3):
+            for d in range(D):
                 wn[d] = (-grad[d] / mag * isb).astype(np.float32)
         else:
-            # discrete neighbour counting, non-periodic bounds (fe_wetting.py:152-178)
-            nx, ny, nz = shape
-            for ix, iy, iz in np.argwhere(isb):
-                normal = np.zeros(3)
+            # discrete neighbour counting, non-periodic bounds (fe_wetting.py:152-203)
+            for x in np.argwhere(isb):
+                normal = np.zeros(D)
                 count = 0
-                for i in range(1, Q):
-                    jx, jy, jz = ix + E[i, 0], iy + E[i, 1], iz + E[i, 2]
-                    if 0 <= jx < nx and 0 <= jy < ny and 0 <= jz < nz and solid[jx, jy, jz]:
-                        normal -= E[i]
+                for i in range(1, Q_):
+                    j = x + E_[i]
+                    if all(0 <= j[d] < shape[d] for d in range(D)) and solid[tuple(j)]:
+                        normal -= E_[i]
                         count += 1
                 if count > 0:
                     normal /= count
-                    norm = np.sqrt(normal[0] ** 2 + normal[1] ** 2 + normal[2] ** 2)
+                    acc = normal[0] ** 2
+                    for d in range(1, D):
+                        acc = acc + normal[d] ** 2
+                    norm = np.sqrt(acc)
                     if norm > 1e-10:
                         normal /= norm
-                wn[:, ix, iy, iz] = normal
+                wn[(slice(None),) + tuple(x)] = normal
         self.wall_normal = wn
 
         # near-wall distance: 11 passes of periodic face-neighbour min-plus (fe_wetting.py:280-311)
@@ -148,7 +162,7 @@ class OracleWetting:
         dist[isb] = 0.0
         for _ in range(int(2 * XI_NEAR_WALL) + 1):
             new = dist.copy()
-            for d in range(3):
+            for d in range(D):
                 for s in (-1, 1):
                     new = np.minimum(new, np.roll(dist, s, axis=d) + np.float32(1.0))
             dist = new
@@ -163,7 +177,7 @@ class OracleWetting:
         # wall normal (round half to even, clamped to the grid, not periodic),
         # and whether it is fluid (fe_wetting.py:313-367)
         bnd = np.argwhere(isb)
-        shift = np.rint(np.stack([wn[d][isb] for d in range(3)], axis=1)).astype(np.int64)
+        shift = np.rint(np.stack([wn[d][isb] for d in range(D)], axis=1)).astype(np.int64)
         nsw = np.clip(bnd + shift, 0, np.array(shape) - 1)
         self.bnd_flat = np.ravel_multi_index(bnd.T, shape)
         self.nsw_flat = np.ravel_multi_index(nsw.T, shape)
@@ -171,14 +185,14 @@ class OracleWetting:
         self.cubic_a = 6.0 * self.sigma * math.cos(math.radians(self.theta_deg)) / self.kappa
 
         # per-direction ghost masks and n.e_i in float32 (fe_wetting.py:221-240)
-        self.ghost_mask = [None] * Q
-        self.n_dot_e = [None] * Q
-        for i in range(1, Q):
-            m = _shift_from(solid, E[i]) & isb
+        self.ghost_mask = [None] * Q_
+        self.n_dot_e = [None] * Q_
+        for i in range(1, Q_):
+            m = _shift_from(solid, E_[i]) & isb
             if m.any():
                 nde = np.zeros(shape, dtype=np.float32)
-                for d in range(3):
-                    nde = nde + wn[d] * np.float32(E[i, d])
+                for d in range(D):
+                    nde = nde + wn[d] * np.float32(E_[i, d])
                 self.ghost_mask[i] = m
                 self.n_dot_e[i] = nde
 
@@ -249,7 +263,8 @@ class OracleWetting:
 # The solver restatement (lbm/fe_ac_solver.py:54-639)
 # ---------------------------------------------------------------------------
 class OracleSolver:
-    """numpy restatement of AllenCahnSolver for 3-D D3Q19 grids.
+    """numpy restatement of AllenCahnSolver: D3Q19 on 3-D grids, D2Q9 on
+    2-D grids (nz == 1, shape (nx, ny)).
 
     ``cfg`` is any object with the FEConfig fields (nx, ny, nz, rho_l, rho_g,
     sigma, xi, beta, kappa, phi_c, tau_l, tau_g, tau_h, theta_eq, g_force).
@@ -262,7 +277,9 @@ class OracleSolver:
         self.cfg = cfg
         self.T = np.dtype(dtype).type
         T = self.T
-        self.shape = (cfg.nx, cfg.ny, cfg.nz)
+        self.shape = (cfg.nx, cfg.ny) if cfg.nz == 1 else (cfg.nx, cfg.ny, cfg.nz)
+        self.D = len(self.shape)
+        self.E, W32_, self.OPP, self.Q = lattice_tables(self.D)
         self.stab_mode = 'fakhari' if stab_mode == 'auto' else stab_mode
         self.boundary_relax = boundary_relax
         self.ghost_scale = ghost_scale
@@ -275,8 +292,8 @@ class OracleSolver:
         self.mu_drive = mu_drive
         self.direct_wetting = direct_wetting
         self.rho_floor = 0.5 * cfg.rho_l
-        self.w = W32.astype(T)
-        self.w_view = self.w.reshape(Q, 1, 1, 1)
+        self.w = W32_.astype(T)
+        self.w_view = self.w.reshape((self.Q,) + (1,) * self.D)
         self.tau_f = cfg.tau_h if cfg.tau_h > 0 else cfg.tau_l
         self.tau_g = cfg.tau_g
         self.step_count = 0
@@ -324,7 +341,7 @@ class OracleSolver:
         T = self.T
         phi = np.asarray(phi_init).astype(T)
         u = (np.asarray(u_init).astype(T) if u_init is not None
-             else np.zeros((3,) + self.shape, dtype=T))
+             else np.zeros((self.D,) + self.shape, dtype=T))
         self.phi = np.clip(phi, T(0), T(1))
         self.rho = self.phi * self.cfg.rho_l + (1.0 - self.phi) * self.cfg.rho_g
         self.u = u
@@ -341,16 +358,17 @@ class OracleSolver:
         """Fused isotropic gradient + laplacian with ghost correction
         (lbm/fe_ac_solver.py:296-320)."""
         T = self.T
-        grad = np.zeros((3,) + self.shape, dtype=T)
+        E = self.E
+        grad = np.zeros((self.D,) + self.shape, dtype=T)
         lap = np.zeros(self.shape, dtype=T)
         w_over_cs2 = self.w / CS2
-        for i in range(1, Q):
+        for i in range(1, self.Q):
             ps = _shift_from(phi, E[i])
             if self.wetting is not None:
                 ps = self.wetting.correct_shifted(phi, ps, i)
             diff = ps - phi
             wi = w_over_cs2[i]
-            for d in range(3):
+            for d in range(self.D):
                 if E[i, d] != 0:
                     grad[d] = grad[d] + (wi * T(E[i, d])) * ps
             lap = lap + (2.0 * wi) * diff
@@ -361,12 +379,13 @@ class OracleSolver:
         itself (lbm/fe_ac_solver.py:267-280): per direction i, per axis d with
         e_id != 0, grad_d += ((w_i e_id) v(x + e_i)) / cs2."""
         T = self.T
-        grad = np.zeros((3,) + self.shape, dtype=T)
-        for i in range(1, Q):
+        E = self.E
+        grad = np.zeros((self.D,) + self.shape, dtype=T)
+        for i in range(1, self.Q):
             vs = _shift_from(v, E[i])
             if self.wetting is not None:
                 vs = self.wetting.correct_shifted(v, vs, i)
-            for d in range(3):
+            for d in range(self.D):
                 if E[i, d] != 0:
                     grad[d] = grad[d] + ((self.w[i] * T(E[i, d])) * vs) / CS2
         return grad
@@ -376,8 +395,8 @@ class OracleSolver:
         ((2 w_i) (phi_i - phi)) / cs2 per direction."""
         T = self.T
         lap = np.zeros(self.shape, dtype=T)
-        for i in range(1, Q):
-            ps = _shift_from(phi, E[i])
+        for i in range(1, self.Q):
+            ps = _shift_from(phi, self.E[i])
             if self.wetting is not None:
                 ps = self.wetting.correct_shifted(phi, ps, i)
             lap = lap + (2.0 * self.w[i]) * (ps - phi) / CS2
@@ -399,10 +418,11 @@ class OracleSolver:
     def _eu(self, v):
         """einsum('qd,d...->q...', e, v): at most two non-zero terms per row."""
         T = self.T
-        out = np.empty((Q,) + v.shape[1:], dtype=T)
-        for i in range(Q):
+        E = self.E
+        out = np.empty((self.Q,) + v.shape[1:], dtype=T)
+        for i in range(self.Q):
             acc = None
-            for d in range(3):
+            for d in range(self.D):
                 if E[i, d] != 0:
                     t = v[d] if E[i, d] > 0 else -v[d]
                     acc = t if acc is None else acc + t
@@ -431,7 +451,7 @@ class OracleSolver:
         mass and drop the previous phi u."""
         T = self.T
         if u_impact is None:
-            u_impact = (0.0, 0.0, 0.0)
+            u_impact = (0.0,) * self.D
         mesh = np.meshgrid(*[np.arange(n) for n in self.shape], indexing="ij")
         dist = np.sqrt(sum((M - center[d]) ** 2 for d, M in enumerate(mesh)))
         C = np.clip(0.5 + 0.5 * np.tanh(2.0 * (radius - dist) / xi), 0.0, 1.0).astype(np.float32).astype(T)
@@ -442,7 +462,7 @@ class OracleSolver:
             phi = np.where(self.solid, T(0), phi)
         self.phi = phi.astype(T)
         self.rho = self.phi * self.cfg.rho_l + (1.0 - self.phi) * self.cfg.rho_g
-        u_new = np.stack([np.full(self.shape, u_impact[d], dtype=T) for d in range(3)])
+        u_new = np.stack([np.full(self.shape, u_impact[d], dtype=T) for d in range(self.D)])
         u = (T(1) - C)[None] * self.u + C[None] * u_new
         if self.solid_any:
             u = np.where(self.solid[None], T(0), u)
@@ -459,6 +479,7 @@ class OracleSolver:
     def step(self):
         T = self.T
         cfg = self.cfg
+        E, Q, OPP, D = self.E, self.Q, self.OPP, self.D
         # 1. phi recovery
         phi = np.clip(_seqsum(self.f), T(0), T(1))
         if self.solid_any:
@@ -478,8 +499,8 @@ class OracleSolver:
         # 4. non-equilibrium stress with new P, old u
         g_neq = self.g - self._g_eq(self.P, self.u)
         sig = {}
-        for a in range(3):
-            for b in range(3):
+        for a in range(D):
+            for b in range(D):
                 acc = None
                 for i in range(Q):
                     c = int(E[i, a] * E[i, b])
@@ -493,12 +514,15 @@ class OracleSolver:
         F_s = self.mu_phi[None] * grad
         Fp = -self.P[None] * drho * CS2 * grad
         visc = (0.5 - self.tau_g) / self.tau_g
-        m = np.stack([(sig[a, 0] * grad[0] + sig[a, 1] * grad[1]) + sig[a, 2] * grad[2]
-                      for a in range(3)])
+        if D == 3:
+            m = np.stack([(sig[a, 0] * grad[0] + sig[a, 1] * grad[1]) + sig[a, 2] * grad[2]
+                          for a in range(3)])
+        else:
+            m = np.stack([sig[a, 0] * grad[0] + sig[a, 1] * grad[1] for a in range(2)])
         Fm = visc * m * drho
-        gf = tuple(cfg.g_force[:3])
+        gf = tuple(cfg.g_force[:D])
         if any(x != 0 for x in gf):
-            F_body = np.asarray(gf, dtype=T).reshape(3, 1, 1, 1) * self.rho[None]
+            F_body = np.asarray(gf, dtype=T).reshape((D,) + (1,) * D) * self.rho[None]
         else:
             F_body = np.zeros_like(F_s)
         if self.stab_mode == 'fakhari':
@@ -510,7 +534,7 @@ class OracleSolver:
         # 6. velocity
         u_from_g = np.stack([_seqsum(np.stack([self.g[i] if E[i, d] > 0 else -self.g[i]
                                                for i in range(Q) if E[i, d] != 0]))
-                             for d in range(3)])
+                             for d in range(D)])
         u = u_from_g + 0.5 * F / rho_eff[None]
         if self.solid_any:
             u = np.where(self.solid[None], T(0), u)
@@ -589,7 +613,7 @@ class OracleSolver:
             m = wt.is_boundary
             phi_b = self.phi[m].copy()
             n_w = wt.wall_normal.astype(T)
-            nz_abs = np.abs(n_w[2])
+            nz_abs = np.abs(n_w[D - 1])
             nmag = np.maximum(np.sqrt(_seqsum(n_w * n_w)), T(1e-10))
             top = (nz_abs[m] / nmag[m]) > 0.5
             inside = (phi_b > 0.15) & (phi_b < 0.85)
@@ -631,7 +655,10 @@ def measure_spread(phi, solid=None):
         return out
     co = np.argwhere(iface)
     mn, mx = co.min(0), co.max(0)
-    Dx, Dy, Dz = (float(mx[a] - mn[a] + 1) for a in range(3))
+    ext = [float(mx[a] - mn[a] + 1) for a in range(c.ndim)]
+    Dx, Dy = ext[0], ext[1]
+    Dz = ext[2] if c.ndim == 3 else 0.0
+    # z_com: centre of the interface along the last axis (the wall-normal one)
     out.update(Dx=Dx, Dy=Dy, Dz=Dz, k=Dx / Dy if Dy > 0 else 0.0,
-               z_com=float(co[:, 2].mean()), count=int(co.shape[0]))
+               z_com=float(co[:, -1].mean()), count=int(co.shape[0]))
     return out

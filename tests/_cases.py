@@ -16,8 +16,9 @@ def inputs(case):
     nx, ny, nz = case["grid"]
     sub = case["substrate"]
     if sub[0] == "flat_z2":
-        solid = np.zeros((nx, ny, nz), dtype=bool)
-        solid[:, :, :2] = True
+        # two wall layers at the bottom of the last axis (z in 3-D, y in 2-D)
+        solid = np.zeros((nx, ny) if nz == 1 else (nx, ny, nz), dtype=bool)
+        solid[..., :2] = True
         frac = solid.astype(np.float32)
     elif sub[0] == "fraction":
         solid, frac = create_substrate_with_fraction(nx, ny, nz, sub[1], R_star=sub[2], R_d=sub[3])

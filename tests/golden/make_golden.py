@@ -93,6 +93,35 @@ CASES = {
         grid=(48, 44, 40), substrate=("fraction", "ridge", 1.0, 6.0), drop=dict(center=(24, 22, 15), radius=6.0, u=(0, 0, -0.05)),
         cfg=dict(theta_eq=162.0), kw=dict(geo_amplification=1.5, geometric_wetting=True),
         dtypes=("float32",), ckpt=(100,), save_f=False, every=10),
+    # 2-D (nz = 1, D2Q9) grids: the wall at the bottom of y.
+    "flat2d_q120": dict(
+        grid=(48, 40, 1), substrate=("flat_z2",), drop=dict(center=(24, 11), radius=8.0, u=(0, 0)),
+        cfg=dict(theta_eq=120.0), kw=dict(geo_amplification=1.5, geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=True),
+    "ridge2d_l162": dict(
+        grid=(64, 48, 1), substrate=("fraction", "ridge", 1.0, 8.0), drop=dict(center=(32, 19), radius=8.0, u=(0, -0.05)),
+        cfg=dict(theta_eq=162.0), kw=dict(geo_amplification=1.5, geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "discrete2d_l150": dict(
+        grid=(64, 48, 1), substrate=("mask", "convex", 4.0 / 3.0, 8.0), drop=dict(center=(32, 30), radius=8.0, u=(0, -0.06)),
+        cfg=dict(theta_eq=150.0, tau_h=0.57), kw=dict(geo_amplification=1.5, geometric_wetting=True, boundary_relax=0.0),
+        dtypes=("float32",), ckpt=(1, 5), save_f=False),
+    "concave2d_q100_tau": dict(
+        grid=(64, 48, 1), substrate=("fraction", "concave", 1.0, 10.0), drop=dict(center=(32, 18), radius=8.0, u=(0.01, -0.04)),
+        cfg=dict(theta_eq=100.0, tau_g=0.6, g_force=(0.0, -1e-6, 0.0)), kw=dict(stab_mode="liang"),
+        dtypes=("float32",), ckpt=(1, 5), save_f=False),
+    "ch2d_q120": dict(
+        grid=(48, 40, 1), substrate=("flat_z2",), drop=dict(center=(24, 11), radius=8.0, u=(0, -0.01)),
+        cfg=dict(theta_eq=120.0), kw=dict(interface_mode="cahn-hilliard", geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "direct2d_l150": dict(
+        grid=(64, 48, 1), substrate=("fraction", "ridge", 1.0, 8.0), drop=dict(center=(32, 15), radius=8.0, u=(0, -0.05)),
+        cfg=dict(theta_eq=150.0), kw=dict(direct_wetting=True, mu_drive=0.5, geo_amplification=1.5, geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "ridge2d_long": dict(
+        grid=(128, 64, 1), substrate=("fraction", "ridge", 1.0, 8.0), drop=dict(center=(64, 19), radius=8.0, u=(0, -0.05)),
+        cfg=dict(theta_eq=162.0), kw=dict(geo_amplification=1.5, geometric_wetting=True),
+        dtypes=("float32",), ckpt=(200,), save_f=False, every=20),
     # The 64x64x48 flat-wall, theta=120 static droplet case, full 500-step run.
     "cfg1_flat64": dict(
         grid=(64, 64, 48), substrate=("flat_z2",), drop=dict(center=(32, 32, 14), radius=12.0, u=(0, 0, 0)),
@@ -107,8 +136,9 @@ def build_inputs(ref, case):
     nx, ny, nz = case["grid"]
     sub = case["substrate"]
     if sub[0] == "flat_z2":
-        solid = np.zeros((nx, ny, nz), dtype=bool)
-        solid[:, :, :2] = True
+        # two wall layers at the bottom of the last axis (z in 3-D, y in 2-D)
+        solid = np.zeros((nx, ny) if nz == 1 else (nx, ny, nz), dtype=bool)
+        solid[..., :2] = True
         frac = solid.astype(np.float32)
     elif sub[0] == "fraction":
         solid, frac = ref["substrate"].create_substrate_with_fraction(

@@ -62,7 +62,7 @@ def test_steps_match_reference(name, dn):
                 assert np.abs(s.rho - gd[f"s{k}_rho"]).max() <= trho
 
 
-@pytest.mark.parametrize("name", ["flat_q120_long", "ridge_l162_long"])
+@pytest.mark.parametrize("name", ["flat_q120_long", "ridge_l162_long", "ridge2d_long"])
 def test_long_runs_match_reference(name):
     case, gd, s = _run(name, "float32")
     tp, tu = TOL[("float32", "long")][:2]
