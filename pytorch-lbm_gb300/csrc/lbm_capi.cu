@@ -47,6 +47,17 @@ cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, c
 template <typename T, typename S>
 cudaError_t launch_mu(const Consts<T>&, const State<T, S>&, cudaStream_t);
 
+// the 2-D (nz == 1, D2Q9) form (lbm_kernels2d.cu)
+template <typename T, typename Src>
+cudaError_t launch_init2d(const Consts<T>&, const State<T, T>&, const Src*, const Src*, cudaStream_t);
+template <typename T>
+cudaError_t launch_step2d(const Consts<T>&, const State<T, T>&, bool, bool, double, cudaStream_t, cudaEvent_t);
+template <typename T>
+cudaError_t launch_observe2d(const Consts<T>&, const State<T, T>&, bool, unsigned, int, T*, T*, T*, T*, T*, T*,
+                             cudaStream_t);
+template <typename T>
+cudaError_t launch_populations2d(const Consts<T>&, const State<T, T>&, bool, T*, T*, cudaStream_t);
+
 template <typename T, typename S>
 size_t case_desc_bytes();
 template <typename T, typename S>
@@ -349,6 +360,50 @@ const Consts<float>& consts_of<float>(const LbmHandle& h) { return h.kf; }
 template <>
 const Consts<double>& consts_of<double>(const LbmHandle& h) { return h.kd; }
 
+// A grid with nz == 1 is 2-D: D2Q9 populations, two velocity components.
+bool is2d(const LbmHandle* h) { return h->nz == 1; }
+int nq_of(int64_t nz) { return nz == 1 ? kQ2 : Q; }
+int ndim_of(int64_t nz) { return nz == 1 ? 2 : 3; }
+
+// The 2-D step of the handle's current state (no bookkeeping).
+template <typename T>
+int launch_next2d(LbmHandle* h, cudaStream_t st, cudaEvent_t mid) {
+  State<T, T> s = make_state<T, T>(*h, h->cur, h->pc);
+  s.c_prev = h->c_last;
+  s.c_cur = h->c_last ^ 1;
+  const double tau_f = h->prm.tau_h > 0 ? h->prm.tau_h : h->prm.tau_l;
+  CUDA_TRY(launch_step2d<T>(consts_of<T>(*h), s, h->raw, h->first, 1.0 - 0.5 / tau_f, st, mid));
+  return LBM_OK;
+}
+
+// The spread reduction runs over a 2-D grid as the 1 x nx x ny grid of the
+// same memory layout, so that its last-axis centre is the centre along y
+// (the wall-normal axis in 2-D); remap_measure2d puts the results back in
+// x, y order: Dz = 0 as the reference reports for 2-D fields, and the
+// z extents of ext6 (if given) 0 or -1 when the set is empty.
+void measure_grid(const LbmHandle* h, int* mx, int* my, int* mz) {
+  if (is2d(h)) {
+    *mx = 1;
+    *my = (int)h->nx;
+    *mz = (int)h->ny;
+  } else {
+    *mx = (int)h->nx;
+    *my = (int)h->ny;
+    *mz = (int)h->nz;
+  }
+}
+void remap_measure2d(double* out9, double* ext6) {
+  const bool any = out9[7] > 0.0;
+  out9[2] = out9[3];
+  out9[3] = out9[4];
+  out9[4] = 0.0;
+  out9[5] = out9[3] > 0.0 ? out9[2] / out9[3] : 0.0;
+  if (ext6) {
+    for (int j = 0; j < 4; ++j) ext6[j] = ext6[j + 2];
+    ext6[4] = ext6[5] = any ? 0.0 : -1.0;
+  }
+}
+
 bool omega1_of(const LbmHandle* h) {
   return h->prec == LBM_F64 ? consts_of<double>(*h).omega_f == 1.0 : consts_of<float>(*h).omega_f == 1.0f;
 }
@@ -419,7 +474,13 @@ template <typename T, typename S>
 int do_step(LbmHandle* h, int nsteps, cudaStream_t st, cudaEvent_t* ev = nullptr) {
   for (int i = 0; i < nsteps; ++i) {
     if (ev) CUDA_TRY(cudaEventRecord(ev[2 * i], st));
-    const int rc = launch_next<T, S>(h, h->tiling, st, ev ? ev[2 * i + 1] : nullptr);
+    int rc;
+    if constexpr (sizeof(S) == sizeof(T)) {
+      rc = is2d(h) ? launch_next2d<T>(h, st, ev ? ev[2 * i + 1] : nullptr)
+                   : launch_next<T, S>(h, h->tiling, st, ev ? ev[2 * i + 1] : nullptr);
+    } else {
+      rc = launch_next<T, S>(h, h->tiling, st, ev ? ev[2 * i + 1] : nullptr);
+    }
     if (rc != LBM_OK) return rc;
     h->last_raw_in = h->raw;
     h->obs_init = false;
@@ -474,7 +535,7 @@ Sizes sizes_of(int64_t nx, int64_t ny, int64_t nz, int precision) {
   const size_t max_tiles = (size_t)((nx + 1) / 2) * (size_t)((ny + 1) / 2) * (size_t)((nz + 1) / 2);
   const size_t npart = std::max<size_t>({(size_t)nblocks, max_tiles, (size_t)kMeasureBlocks * kMeasVals});
   Sizes z;
-  z.pop = (size_t)Q * Np * P;  // one of f[0], f[1], g[0], g[1]
+  z.pop = (size_t)nq_of(nz) * Np * P;  // one of f[0], f[1], g[0], g[1]
   z.u = 3 * Np * T;
   z.phi = Np * T;  // phi and class arrays padded to Np like the populations
   z.eps = N * T;
@@ -495,7 +556,8 @@ const char* lbm_last_error(void) { return g_err.c_str(); }
 
 int lbm_footprint(int64_t nx, int64_t ny, int64_t nz, int precision, int64_t* bytes) {
   if (!bytes) return fail(LBM_E_ARG, "lbm_footprint: null argument");
-  if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_footprint: 3-D grids with every extent >= 2 only");
+  if (nx < 2 || ny < 2 || nz < 1 || nz == 1 && precision == LBM_F16)
+    return fail(LBM_E_UNSUPPORTED, "lbm_footprint: 3-D grids with every extent >= 2, or 2-D grids (nz == 1) in LBM_F32 or LBM_F64");
   if (precision != LBM_F32 && precision != LBM_F64 && precision != LBM_F16)
     return fail(LBM_E_ARG, "lbm_footprint: bad precision");
   *bytes = (int64_t)sizes_of(nx, ny, nz, precision).total();
@@ -507,9 +569,12 @@ const char* lbm_version(void) { return "lbm_gb300 0.1 (sm_103a)"; }
 int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int precision, LbmHandle** out) {
   if (!params || !out) return fail(LBM_E_ARG, "lbm_create: null argument");
   *out = nullptr;
-  if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_create: 3-D grids with every extent >= 2 only");
+  if (nx < 2 || ny < 2 || nz < 1)
+    return fail(LBM_E_UNSUPPORTED, "lbm_create: 3-D grids with every extent >= 2, or 2-D grids (nz == 1) only");
   if (precision != LBM_F32 && precision != LBM_F64 && precision != LBM_F16)
     return fail(LBM_E_ARG, "lbm_create: precision must be LBM_F32, LBM_F64 or LBM_F16");
+  if (nz == 1 && precision == LBM_F16)
+    return fail(LBM_E_UNSUPPORTED, "lbm_create: 2-D grids (nz == 1) run in LBM_F32 or LBM_F64");
   const int64_t N = nx * ny * nz;
   const int64_t Np = (N + kAlignNodes - 1) / kAlignNodes * kAlignNodes;
   if (Np * Q > (int64_t)0x7fffffff) return fail(LBM_E_ARG, "lbm_create: grid too large (19 N must be < 2^31)");
@@ -673,7 +738,7 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
     CUDA_TRY(cudaMemcpyAsync(stage, phi, N * es, cudaMemcpyHostToDevice, st));
     dphi = stage;
     if (u) {
-      CUDA_TRY(cudaMemcpyAsync(stage + N * es, u, 3 * N * es, cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(stage + N * es, u, ndim_of(h->nz) * N * es, cudaMemcpyHostToDevice, st));
       du = stage + N * es;
     }
   }
@@ -681,6 +746,12 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
     using T = typename decltype(tag)::T;
     using S = typename decltype(tag)::S;
     State<T, S> s = make_state<T, S>(*h, in, h->pc ^ 1);
+    if constexpr (sizeof(S) == sizeof(T)) {
+      if (is2d(h))
+        return src_dtype == LBM_DT_F32
+                   ? launch_init2d<T, float>(consts_of<T>(*h), s, (const float*)dphi, (const float*)du, st)
+                   : launch_init2d<T, double>(consts_of<T>(*h), s, (const double*)dphi, (const double*)du, st);
+    }
     return src_dtype == LBM_DT_F32
                ? launch_init<T, S, float>(consts_of<T>(*h), s, (const float*)dphi, (const float*)du, st)
                : launch_init<T, S, double>(consts_of<T>(*h), s, (const double*)dphi, (const double*)du, st);
@@ -741,6 +812,7 @@ int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3)
 
 int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz) {
   if (!h) return fail(LBM_E_ARG, "lbm_set_tile: null handle");
+  if (is2d(h) && (tx || ty || tz)) return fail(LBM_E_UNSUPPORTED, "lbm_set_tile: 2-D grids run the per-node kernels only");
   if (tx == 1 || ty == 1 || tz == 1 || tx < 0 || ty < 0 || tz < 0 || tx > 64 || ty > 64 || tz > 256)
     return fail(LBM_E_ARG, "lbm_set_tile: tile extents must be in [2, 64] x [2, 64] x [2, 256] (0 = automatic)");
   Tiling t = make_tiling(h->nx, h->ny, h->nz, tx, ty, tz, h->prec);
@@ -754,6 +826,7 @@ int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz) {
 
 int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* best_ms) {
   if (!h) return fail(LBM_E_ARG, "lbm_autotune: null handle");
+  if (is2d(h)) return fail(LBM_E_UNSUPPORTED, "lbm_autotune: 2-D grids have no launch parameters to tune");
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_autotune: call lbm_init_fields first");
   if (reps <= 0) reps = 5;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -852,6 +925,11 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u, v
     using S = typename decltype(tag)::S;
     State<T, S> s = make_state<T, S>(*h, in_buf, h->pc ^ 1);
     s.c_cur = h->c_last;
+    if constexpr (sizeof(S) == sizeof(T)) {
+      if (is2d(h))
+        return launch_observe2d<T>(consts_of<T>(*h), s, h->last_raw_in, mask, mode, (T*)phi, (T*)rho, (T*)u,
+                                   (T*)P, (T*)p, (T*)mu, st);
+    }
     return launch_observe<T, S>(consts_of<T>(*h), s, h->last_raw_in, mask, mode, (T*)phi, (T*)rho, (T*)u,
                                 (T*)P, (T*)p, (T*)mu, st);
   });
@@ -864,6 +942,7 @@ int lbm_inject_droplet(LbmHandle* h, const double* center3, double radius, doubl
   if (!h || !center3) return fail(LBM_E_ARG, "lbm_inject_droplet: null argument");
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_inject_droplet: call lbm_init_fields first");
   if (!(radius >= 0.0) || !(xi > 0.0)) return fail(LBM_E_ARG, "lbm_inject_droplet: radius >= 0 and xi > 0 required");
+  if (is2d(h)) return fail(LBM_E_UNSUPPORTED, "lbm_inject_droplet: 3-D grids only");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   InjectParams ip;
   std::memset(&ip, 0, sizeof(ip));
@@ -921,6 +1000,9 @@ int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream) {
     using S = typename decltype(tag)::S;
     State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
     s.c_prev = h->c_last;
+    if constexpr (sizeof(S) == sizeof(T)) {
+      if (is2d(h)) return launch_populations2d<T>(consts_of<T>(*h), s, h->raw, (T*)f, (T*)g, st);
+    }
     return launch_populations<T, S>(consts_of<T>(*h), s, h->raw, (T*)f, (T*)g, st);
   });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_get_populations: ") + cudaGetErrorString(e));
@@ -934,7 +1016,7 @@ int lbm_get_geometry(LbmHandle* h, uint8_t* node_class, uint8_t* is_boundary, fl
   const size_t N = (size_t)h->N;
   if (node_class) std::memcpy(node_class, h->geo.cls.data(), N);
   if (is_boundary) std::memcpy(is_boundary, h->geo.boundary.data(), N);
-  if (wall_normal) std::memcpy(wall_normal, h->geo.wall_normal.data(), 3 * N * sizeof(float));
+  if (wall_normal) std::memcpy(wall_normal, h->geo.wall_normal.data(), ndim_of(h->nz) * N * sizeof(float));
   if (wall_weight) std::memcpy(wall_weight, h->geo.wall_weight.data(), N * sizeof(float));
   if (near_wall) std::memcpy(near_wall, h->geo.near_wall.data(), N);
   if (partial) std::memcpy(partial, h->geo.partial.data(), N);
@@ -946,7 +1028,8 @@ int lbm_geometry_host(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid, 
                       uint8_t* is_boundary, float* wall_normal, float* wall_weight, uint8_t* near_wall,
                       uint8_t* partial) {
   if (!solid) return fail(LBM_E_ARG, "lbm_geometry_host: null solid");
-  if (nx < 2 || ny < 2 || nz < 2) return fail(LBM_E_UNSUPPORTED, "lbm_geometry_host: 3-D grids only");
+  if (nx < 2 || ny < 2 || nz < 1)
+    return fail(LBM_E_UNSUPPORTED, "lbm_geometry_host: 3-D grids with every extent >= 2, or 2-D grids (nz == 1) only");
   if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
     return fail(LBM_E_ARG, "lbm_geometry_host: fraction and fraction_dtype disagree");
   Geometry g;
@@ -955,7 +1038,7 @@ int lbm_geometry_host(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid, 
   const size_t N = (size_t)(nx * ny * nz);
   if (node_class) std::memcpy(node_class, g.cls.data(), N);
   if (is_boundary) std::memcpy(is_boundary, g.boundary.data(), N);
-  if (wall_normal) std::memcpy(wall_normal, g.wall_normal.data(), 3 * N * sizeof(float));
+  if (wall_normal) std::memcpy(wall_normal, g.wall_normal.data(), ndim_of(nz) * N * sizeof(float));
   if (wall_weight) std::memcpy(wall_weight, g.wall_weight.data(), N * sizeof(float));
   if (near_wall) std::memcpy(near_wall, g.near_wall.data(), N);
   if (partial) std::memcpy(partial, g.partial.data(), N);
@@ -993,15 +1076,18 @@ int lbm_measure(LbmHandle* h, double* out9, void* stream) {
   int rc = lbm_get_fields(h, LBM_FIELD_PHI, h->meas_phi, nullptr, nullptr, nullptr, nullptr, nullptr, stream);
   if (rc) return rc;
   cudaError_t e;
+  int mx, my, mz;
+  measure_grid(h, &mx, &my, &mz);
   if (h->prec != LBM_F64)
-    e = launch_measure<float>((int)h->nx, (int)h->ny, (int)h->nz, (const float*)h->meas_phi, h->cls, h->partials,
-                              kMeasureBlocks, h->counters + 1, h->scal + 2, st);
+    e = launch_measure<float>(mx, my, mz, (const float*)h->meas_phi, h->cls, h->partials, kMeasureBlocks,
+                              h->counters + 1, h->scal + 2, st);
   else
-    e = launch_measure<double>((int)h->nx, (int)h->ny, (int)h->nz, (const double*)h->meas_phi, h->cls, h->partials,
-                               kMeasureBlocks, h->counters + 1, h->scal + 2, st);
+    e = launch_measure<double>(mx, my, mz, (const double*)h->meas_phi, h->cls, h->partials, kMeasureBlocks,
+                               h->counters + 1, h->scal + 2, st);
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_measure: ") + cudaGetErrorString(e));
   CUDA_TRY(cudaMemcpyAsync(out9, h->scal + 2, 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
+  if (is2d(h)) remap_measure2d(out9, nullptr);
   return LBM_OK;
 }
 
@@ -1037,7 +1123,7 @@ struct StatePart {
   size_t bytes;
 };
 std::vector<StatePart> state_parts(LbmHandle* h) {
-  const size_t pop = (size_t)Q * h->Np * h->psize;
+  const size_t pop = (size_t)nq_of(h->nz) * h->Np * h->psize;
   // g of the last step's input buffer: the pressure read-out after a step sums it
   return {{h->f[h->cur], pop},
           {h->g[h->cur], pop},
@@ -1138,7 +1224,9 @@ int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, f
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int rc = lbm_get_fields(h, LBM_FIELD_PHI, h->meas_phi, nullptr, nullptr, nullptr, nullptr, nullptr, stream);
   if (rc) return rc;
-  const int nx = (int)h->nx, ny = (int)h->ny, nz = (int)h->nz, N = (int)h->N, us = (int)h->Np;
+  const int N = (int)h->N, us = (int)h->Np;
+  int nx, ny, nz;
+  measure_grid(h, &nx, &ny, &nz);
   cudaError_t e;
   if (h->prec != LBM_F64) {
     e = launch_measure<float>(nx, ny, nz, (const float*)h->meas_phi, h->cls, h->partials, kMeasureBlocks,
@@ -1157,6 +1245,7 @@ int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, f
   double r[25];
   CUDA_TRY(cudaMemcpyAsync(r, h->scal + 2, sizeof(r), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
+  if (is2d(h)) remap_measure2d(r, r + 14);
   if (sum_phi) *sum_phi = r[0];
   if (cmax) *cmax = (float)r[1];
   if (extents6)
@@ -1350,6 +1439,7 @@ int lbm_batch_create(LbmHandle* const* handles, int n, LbmBatch** out) {
     if (h->mu)
       return fail(LBM_E_UNSUPPORTED, "lbm_batch_create: the gradient-of-mu modes (cahn-hilliard, mu_drive) step "
                                      "one grid at a time");
+    if (is2d(h)) return fail(LBM_E_UNSUPPORTED, "lbm_batch_create: 2-D grids step one grid at a time");
   }
   LbmBatch* b = new (std::nothrow) LbmBatch();
   if (!b) return fail(LBM_E_ARG, "lbm_batch_create: out of host memory");

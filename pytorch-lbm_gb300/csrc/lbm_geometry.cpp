@@ -49,10 +49,12 @@ void parallel_for(int64_t n, Fn fn) {
 // evaluated in the fraction's own type F (fe_wetting.py:242-267).  Every node
 // is computed: off the boundary the product with the mask is a signed zero
 // (-0 where -grad/|grad| is negative or -0), as in the reference's array.
+// A 2-D grid (nz == 1) has two axes; its third component is 0.
 template <typename F>
 void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, int64_t ny, int64_t nz,
                     std::vector<float>& wn) {
   const int64_t N = nx * ny * nz;
+  const bool two_d = nz == 1;
   auto grad_axis = [&](int64_t ix, int64_t iy, int64_t iz, int axis) -> F {
     int64_t n_ax = axis == 0 ? nx : (axis == 1 ? ny : nz);
     int64_t i = axis == 0 ? ix : (axis == 1 ? iy : iz);
@@ -72,16 +74,16 @@ void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, 
         const F mask = bnd[n] ? (F)1 : (F)0;
         const F g0 = grad_axis(ix, iy, iz, 0);
         const F g1 = grad_axis(ix, iy, iz, 1);
-        const F g2 = grad_axis(ix, iy, iz, 2);
+        const F g2 = two_d ? (F)0 : grad_axis(ix, iy, iz, 2);
         F acc = (F)0;
         acc = acc + g0 * g0;
         acc = acc + g1 * g1;
-        acc = acc + g2 * g2;
+        if (!two_d) acc = acc + g2 * g2;
         F mag = std::sqrt(acc);
         if (mag < (F)1e-10) mag = (F)1e-10;
         wn[n] = (float)(((-g0) / mag) * mask);
         wn[N + n] = (float)(((-g1) / mag) * mask);
-        wn[2 * N + n] = (float)(((-g2) / mag) * mask);
+        wn[2 * N + n] = two_d ? 0.0f : (float)(((-g2) / mag) * mask);
       }
   });
 }
@@ -91,6 +93,11 @@ void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, 
 int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in, const void* fraction,
                      int fraction_dtype, bool wetting, bool dbl_precision, Geometry& g) {
   const int64_t N = nx * ny * nz;
+  // nz == 1: a 2-D grid on D2Q9 (its velocities as 3-D vectors with e_z = 0;
+  // the z neighbours of the near-wall search are then the node itself)
+  const bool two_d = nz == 1;
+  const int nq = two_d ? kQ2 : kQ;
+  const int(*E)[3] = two_d ? kE2 : kE;
   g.solid.assign(N, 0);
   for (int64_t n = 0; n < N; ++n) g.solid[n] = solid_in[n] ? 1 : 0;
   g.partial.assign(N, 0);
@@ -127,8 +134,8 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
       for (int64_t iy = 0; iy < ny; ++iy)
         for (int64_t iz = 0; iz < nz; ++iz) {
           if (!g.solid[idx(ix, iy, iz, ny, nz)]) continue;
-          for (int q = 1; q < kQ; ++q) {
-            const int64_t n = idx(wrap(ix + kE[q][0], nx), wrap(iy + kE[q][1], ny), wrap(iz + kE[q][2], nz), ny, nz);
+          for (int q = 1; q < nq; ++q) {
+            const int64_t n = idx(wrap(ix + E[q][0], nx), wrap(iy + E[q][1], ny), wrap(iz + E[q][2], nz), ny, nz);
             if (!g.solid[n]) g.boundary[n] = 1;
           }
         }
@@ -147,13 +154,13 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
             if (!g.boundary[n]) continue;
             double nm[3] = {0.0, 0.0, 0.0};
             int count = 0;
-            for (int q = 1; q < kQ; ++q) {
-              const int64_t jx = ix + kE[q][0], jy = iy + kE[q][1], jz = iz + kE[q][2];
+            for (int q = 1; q < nq; ++q) {
+              const int64_t jx = ix + E[q][0], jy = iy + E[q][1], jz = iz + E[q][2];
               if (jx >= 0 && jx < nx && jy >= 0 && jy < ny && jz >= 0 && jz < nz &&
                   g.solid[idx(jx, jy, jz, ny, nz)]) {
-                nm[0] -= kE[q][0];
-                nm[1] -= kE[q][1];
-                nm[2] -= kE[q][2];
+                nm[0] -= E[q][0];
+                nm[1] -= E[q][1];
+                nm[2] -= E[q][2];
                 ++count;
               }
             }
@@ -203,13 +210,25 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
         g.near_wall[n] = g.dist[n] < 10 ? 1 : 0;  // dist < 2 xi
       }
     }
-    // top-surface flag of the boundary-phi relaxation, |n_z| / |n| > 1/2 in
-    // the solver precision (fe_ac_solver.py:602-606)
+    // top-surface flag of the boundary-phi relaxation, |n_last| / |n| > 1/2
+    // in the solver precision, n_last the component along the last axis (z,
+    // or y on a 2-D grid) (fe_ac_solver.py:602-606)
     for (int64_t n = 0; n < N; ++n) {
       if (!g.boundary[n]) continue;
       const float a = g.wall_normal[n], b = g.wall_normal[N + n], c = g.wall_normal[2 * N + n];
       bool top;
-      if (dbl_precision) {
+      if (two_d) {
+        if (dbl_precision) {
+          const double x = a, y = b;
+          double m = std::sqrt(x * x + y * y);
+          if (m < 1e-10) m = 1e-10;
+          top = std::fabs(y) / m > 0.5;
+        } else {
+          float m = std::sqrt(a * a + b * b);
+          if (m < 1e-10f) m = 1e-10f;
+          top = std::fabs(b) / m > 0.5f;
+        }
+      } else if (dbl_precision) {
         const double x = a, y = b, z = c;
         double m = std::sqrt((x * x + y * y) + z * z);
         if (m < 1e-10) m = 1e-10;

@@ -17,8 +17,11 @@ the reference holds after the same step.  Each read returns a new tensor.
 (torch tensor or numpy array), as in the reference.  ``interface_mode=
 'cahn-hilliard'`` and ``mu_drive > 0`` add a chemical-potential pass per step
 (float32 / float64); ``direct_wetting`` relaxes top-surface boundary phi towards
-the cubic-wall-energy value.  2-D grids (the reference's D2Q9 path) raise
-``NotImplementedError`` instead of running a different model.
+the cubic-wall-energy value.  A 2-D grid (``nz == 1``) runs the D2Q9 form
+of the same step (csrc/lbm_kernels2d.cu) in float32 or float64, with fields
+of shape ``(nx, ny)`` and ``u`` of shape ``(2, nx, ny)``, as the reference's
+2-D path; it steps one grid at a time (no batches, no fused tiles, no
+``inject_droplet``).
 """
 from __future__ import annotations
 
@@ -29,7 +32,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .lattice import D3Q19
+from .lattice import D2Q9, D3Q19
 
 _STAB = {"fakhari": 0, "liang": 1, "none": 2}
 
@@ -79,8 +82,8 @@ class AllenCahnSolver:
                  boundary_relax=0.3, interface_mode="allen-cahn", ghost_scale=None,
                  sharpen_reduce=0.8, mu_wall_scale=1.0, geometric_wetting=False,
                  direct_wetting=False, ch_wall_blend=0.0, geo_amplification=1.0, ac_scale=1.0):
-        if config.nz == 1:
-            raise NotImplementedError("2-D (D2Q9) grids are not supported by the GB300 solver")
+        if config.nz == 1 and dtype == torch.float16:
+            raise NotImplementedError("2-D (D2Q9) grids run in float32 or float64")
         if interface_mode not in ("allen-cahn", "cahn-hilliard"):
             raise ValueError(f"unknown interface_mode {interface_mode!r}")
         if (interface_mode == "cahn-hilliard" or mu_drive > 0.0) and dtype == torch.float16:
@@ -123,8 +126,8 @@ class AllenCahnSolver:
         self._geo_amplification = geo_amplification
         self._ac_scale = ac_scale
         self.shape = tuple(config.grid_shape)
-        self.ndim = 3
-        self.lattice = D3Q19()
+        self.ndim = len(self.shape)
+        self.lattice = D2Q9() if self.ndim == 2 else D3Q19()
         self.cs2 = self.lattice.cs2
         self._tau_f = config.tau_h if config.tau_h > 0 else config.tau_l
         self._tau_g = config.tau_g
@@ -163,7 +166,7 @@ class AllenCahnSolver:
         self._lib = nat.lib()
         h = ctypes.c_void_p()
         with torch.cuda.device(dev):
-            nat.check(self._lib.lbm_create(ctypes.byref(p), self.shape[0], self.shape[1], self.shape[2],
+            nat.check(self._lib.lbm_create(ctypes.byref(p), config.nx, config.ny, config.nz,
                                            self._prec, ctypes.byref(h)), "lbm_create")
         self._h = h
         if amp_field is not None:
@@ -226,13 +229,13 @@ class AllenCahnSolver:
     def _geometry_tables(self):
         N = int(np.prod(self.shape))
         out = dict(node_class=np.empty(N, np.uint8), is_boundary=np.empty(N, np.bool_),
-                   wall_normal=np.empty((3, N), np.float32), wall_weight=np.empty(N, np.float32),
+                   wall_normal=np.empty((self.ndim, N), np.float32), wall_weight=np.empty(N, np.float32),
                    near_wall=np.empty(N, np.bool_), partial=np.empty(N, np.bool_))
         c = lambda a: a.ctypes.data_as(ctypes.c_void_p)
         nat.check(self._lib.lbm_get_geometry(self._h, c(out["node_class"]), c(out["is_boundary"]),
                                              c(out["wall_normal"]), c(out["wall_weight"]),
                                              c(out["near_wall"]), c(out["partial"])), "lbm_get_geometry")
-        return {k: v.reshape((3,) + self.shape if k == "wall_normal" else self.shape) for k, v in out.items()}
+        return {k: v.reshape((self.ndim,) + self.shape if k == "wall_normal" else self.shape) for k, v in out.items()}
 
     def init_fields(self, phi_init, u_init=None):
         """lbm/fe_ac_solver.py:239-261."""
@@ -259,8 +262,8 @@ class AllenCahnSolver:
             if u_init is not None:
                 uh = u_init.detach().cpu().numpy() if torch.is_tensor(u_init) else np.asarray(u_init)
                 uh = np.ascontiguousarray(uh, dtype=npdt)
-                if uh.shape != (3,) + self.shape:
-                    raise ValueError(f"u shape {uh.shape} != (3,) + grid")
+                if uh.shape != (self.ndim,) + self.shape:
+                    raise ValueError(f"u shape {uh.shape} != ({self.ndim},) + grid")
             # host sources are copied asynchronously: keep them alive until the copy ran
             self._keep = (ph, uh)
             nat.check(self._lib.lbm_init_fields(
@@ -297,6 +300,8 @@ class AllenCahnSolver:
         nodes, the phi-mass reference re-based, no previous phi u."""
         if not self._initialized:
             raise RuntimeError("init_fields must be called before inject_droplet()")
+        if self.ndim == 2:
+            raise NotImplementedError("inject_droplet runs on 3-D grids")
         if u_impact is None:
             u_impact = (0.0,) * 3
         c = (ctypes.c_double * 3)(*[float(x) for x in center])
@@ -321,7 +326,7 @@ class AllenCahnSolver:
             mask = 0
             out = {}
             for k in missing:
-                shp = (3,) + self.shape if k == "u" else self.shape
+                shp = (self.ndim,) + self.shape if k == "u" else self.shape
                 out[k] = torch.empty(shp, dtype=self.dtype, device=self.device)
                 mask |= bits[k]
             nat.check(self._lib.lbm_get_fields(
@@ -361,8 +366,7 @@ class AllenCahnSolver:
 
     def _populations(self):
         if "f" not in self._cache:
-            Q = 19
-            f = torch.empty((Q,) + self.shape, dtype=self.dtype, device=self.device)
+            f = torch.empty((self.lattice.q,) + self.shape, dtype=self.dtype, device=self.device)
             g = torch.empty_like(f)
             nat.check(self._lib.lbm_get_populations(self._h, nat.ptr(f), nat.ptr(g), nat.stream_ptr()),
                       "lbm_get_populations")
@@ -394,7 +398,8 @@ class AllenCahnSolver:
 
     def measure(self, stream=None):
         """Spread diagnostics of the current phi, reduced on the device:
-        volume, C_max, Dx, Dy, Dz, k, z_com, count, has_nan."""
+        volume, C_max, Dx, Dy, Dz, k, z_com, count, has_nan.  On a 2-D grid
+        Dz is 0 and z_com is the centre along y (the wall-normal axis)."""
         out = (ctypes.c_double * 9)()
         nat.check(self._lib.lbm_measure(self._h, out, nat.stream_ptr(stream)), "lbm_measure")
         keys = ("volume", "C_max", "Dx", "Dy", "Dz", "k", "z_com", "count", "has_nan")
@@ -406,7 +411,8 @@ class AllenCahnSolver:
     def reduce(self, stream=None):
         """Global float64 reductions of the current fields on the device:
         sum_phi, momentum (sum rho u, 3 components), extents (first and last
-        x, y, z index of phi > 0.5; -1 when empty), C_max."""
+        x, y, z index of phi > 0.5; -1 when empty), C_max.  On a 2-D grid the
+        z momentum is 0 and the z extents are 0 (-1 when empty)."""
         sp, cm = ctypes.c_double(), ctypes.c_float()
         mom = (ctypes.c_double * 3)()
         ext = (ctypes.c_int32 * 6)()
@@ -486,6 +492,8 @@ class AllenCahnSolver:
         mid-plane slices, in the key layout of the reference's sweep driver
         (scripts/run_thesis_sweep.py:219-243): phi_3d, u_3d, solid_3d, xz_slice,
         yz_slice, xz_solid, step, nx, ny, nz."""
+        if self.ndim == 2:
+            raise NotImplementedError("snapshots in the sweep-driver layout are 3-D")
         phi, vel = self.fields("phi", "u")
         phi_np = phi.detach().cpu().numpy()
         u_np = vel.detach().cpu().numpy()

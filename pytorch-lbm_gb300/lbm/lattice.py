@@ -2,9 +2,8 @@
 
 The velocity ordering, float32 weights and opposite-direction tables are the
 population layout of the reference (pytorch-lbm ``lbm/lattice.py:10-96``); the
-CUDA kernels hard-code the same D3Q19 table (``csrc/lbm_common.cuh``).  D2Q9
-is provided for callers that build or inspect 2-D lattices; the GPU solver
-itself runs 3-D grids only.
+CUDA kernels hard-code the same tables (D3Q19: ``csrc/lbm_common.cuh``, D2Q9
+of the 2-D grids: ``csrc/lbm_kernels2d.cu``).
 """
 import numpy as np
 import torch

@@ -39,6 +39,9 @@ def test_lattice_tables():
     assert np.array_equal(d3.e.numpy(), E.astype(np.float32)) and np.array_equal(d3.w.numpy(), W32)
     assert np.array_equal(d3.opp.numpy(), OPP) and d3.q == 19 and d3.dim == 3
     assert torch.equal(d3.ew, d3.e * d3.w[:, None]) and np.array_equal(d3.stream_shifts, -E)
+    from oracle.ac_oracle import E2, OPP2, W2_32
     d2 = lbm.D2Q9()
     assert d2.q == 9 and d2.dim == 2 and abs(float(d2.w.double().sum()) - 1.0) < 1e-7
     assert np.array_equal(d2.e.numpy()[d2.opp.numpy()], -d2.e.numpy())
+    assert np.array_equal(d2.e.numpy(), E2.astype(np.float32)) and np.array_equal(d2.w.numpy(), W2_32)
+    assert np.array_equal(d2.opp.numpy(), OPP2)

@@ -109,7 +109,7 @@ def test_results_independent_of_tiling(tile):
     assert rel_l2(_np(a.u), _np(b.u)) <= 1e-5
 
 
-@pytest.mark.parametrize("name", ["flat_q120_long", "ridge_l162_long"])
+@pytest.mark.parametrize("name", ["flat_q120_long", "ridge_l162_long", "ridge2d_long"])
 def test_long_runs_vs_reference(name):
     case, s = _gpu(name, "float32")
     gd = golden(name, "float32")

@@ -40,7 +40,8 @@ def _geometry(lib, case, precision):
     N = nx * ny * nz
     solid, frac, _, _ = inputs(case)
     cfg = config(case)
-    o = dict(cls=np.empty(N, np.uint8), bnd=np.empty(N, np.bool_), wn=np.empty((3, N), np.float32),
+    nd = 2 if nz == 1 else 3  # 2-D grids: D2Q9, two normal components
+    o = dict(cls=np.empty(N, np.uint8), bnd=np.empty(N, np.bool_), wn=np.empty((nd, N), np.float32),
              ww=np.empty(N, np.float32), near=np.empty(N, np.bool_), part=np.empty(N, np.bool_))
     c = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     fr = None if frac is None else np.ascontiguousarray(frac)
@@ -50,8 +51,8 @@ def _geometry(lib, case, precision):
                                cfg.kappa, precision, c(o["cls"]), c(o["bnd"]), c(o["wn"]), c(o["ww"]),
                                c(o["near"]), c(o["part"]))
     assert rc == 0, lib.lbm_last_error()
-    shp = (nx, ny, nz)
-    return {k: (v.reshape((3,) + shp) if k == "wn" else v.reshape(shp)) for k, v in o.items()}
+    shp = (nx, ny) if nz == 1 else (nx, ny, nz)
+    return {k: (v.reshape((nd,) + shp) if k == "wn" else v.reshape(shp)) for k, v in o.items()}
 
 
 @pytest.mark.parametrize("name,dn", [(n, d) for n, c in CASES.items() for d in c["dtypes"]])
@@ -83,8 +84,11 @@ def test_argument_errors(built_lib):
     p = nat.LbmParams(rho_l=1.0, rho_g=1 / 828.0, sigma=0.01, xi=4.0, beta=0.03, kappa=0.06,
                       tau_l=0.53, tau_g=0.53, tau_h=1.0, theta_eq=120.0)
     h = ctypes.c_void_p()
-    assert built_lib.lbm_create(ctypes.byref(p), 8, 8, 1, 0, ctypes.byref(h)) == -4
+    assert built_lib.lbm_create(ctypes.byref(p), 8, 8, 0, 0, ctypes.byref(h)) == -4
     assert b"3-D" in built_lib.lbm_last_error()
+    # 2-D grids (nz == 1) run in float32 or float64 only
+    assert built_lib.lbm_create(ctypes.byref(p), 8, 8, 1, nat.LBM_F16, ctypes.byref(h)) == -4
+    assert b"2-D" in built_lib.lbm_last_error()
     assert built_lib.lbm_create(ctypes.byref(p), 8, 8, 8, 7, ctypes.byref(h)) == -1
     assert built_lib.lbm_create(None, 8, 8, 8, 0, ctypes.byref(h)) == -1
     bad = nat.LbmParams(rho_l=1.0, rho_g=1.0, xi=4.0, tau_l=0.5, tau_g=0.53)
