@@ -55,6 +55,14 @@ B_ALG_STEP = {"fp32": 336, "fp16": 184}
 #   k_step    the fused kernel: the whole step
 B_ALG_KERNEL = {"fp32": {"k_phi": 81, "k_update": 257, "k_step": 337},
                 "fp16": {"k_phi": 47, "k_update": 143, "k_step": 185}}
+# 2-D (D2Q9) grids, float32: f and g (2 x 9), u (2), previous phi (1), read
+# and written once: 2 x 4 x 21 = 168 B per node and step.  k2_phi reads f
+# (36) and the class byte and writes phi (4); k2_update reads g (36), u (8),
+# the previous phi (4) and the class byte and writes f, g (72) and u (8).
+# (k2_update also reads f again for the collision: traffic beyond these
+# algorithmic bytes.)
+B_ALG_STEP_2D = 168
+B_ALG_KERNEL_2D = {"k2_phi": 41, "k2_update": 129}
 
 WORKLOADS = {
     "ridge150": dict(grid=(150, 150, 107), substrate=("ridge", 1.0, 22.5), center=(75, 75, 80),
@@ -64,6 +72,10 @@ WORKLOADS = {
                    u=(0.0, 0.0, 0.0), theta=120.0,
                    label="flat 64x64x48 D3Q19 static droplet, theta=120, alpha_geo=1.5"),
     # the large single solve of the precision form: convex hemisphere of radius 60 (R* = 60/45)
+    # a 2-D (D2Q9) grid of about the default case's node count: ridge R* = 1, droplet R = 150
+    "ridge2d": dict(grid=(2048, 1024, 1), substrate=("ridge", 1.0, 150.0), center=(1024, 310), radius=150.0,
+                    u=(0.0, -0.05), theta=162.0,
+                    label="ridge 2048x1024 D2Q9 (2-D) droplet impact, droplet R=150, theta=162, alpha_geo=1.5"),
     "convex384": dict(grid=(384, 384, 256), substrate=("convex", 60.0 / 45.0, 45.0), center=(192, 192, 180),
                       radius=45.0, u=(0.0, 0.0, -0.06), theta=150.0,
                       label="convex 384x384x256 D3Q19 droplet impact, hemisphere R=60, droplet R=45, "
@@ -80,8 +92,8 @@ def make_case(name):
     cfg = FEConfig(nx=nx, ny=ny, nz=nz, rho_l=1.0, rho_g=1.0 / 828.0, sigma=0.01424, xi=4.0,
                    tau_l=0.53, tau_g=0.53, theta_eq=w["theta"], device="cuda", max_steps=2000)
     if w["substrate"][0] == "flat_z2":
-        solid = np.zeros((nx, ny, nz), dtype=bool)
-        solid[:, :, :2] = True
+        solid = np.zeros(tuple(cfg.grid_shape), dtype=bool)
+        solid[..., :2] = True
         frac = solid.astype(np.float32)
     else:
         t, rs, rd = w["substrate"]
@@ -108,8 +120,8 @@ def solver_kwargs(mode, shape):
     m = dict(MODES[mode])
     if "alpha_field" in m:
         lo, hi = m.pop("alpha_field")
-        nx, ny, nz = shape
-        ramp = np.linspace(lo, hi, nx, dtype=np.float32)[:, None, None]
+        nx = shape[0]
+        ramp = np.linspace(lo, hi, nx, dtype=np.float32).reshape((nx,) + (1,) * (len(shape) - 1))
         kw["geo_amplification"] = np.ascontiguousarray(np.broadcast_to(ramp, shape))
     kw.update(m)
     return kw
@@ -251,13 +263,16 @@ def run_ours(args, rank, world, device):
 
     # --- device-resident timed region -------------------------------------
     pdt = torch.float16 if args.precision == "fp16" else torch.float32
-    skw = solver_kwargs(args.mode, (cfg.nx, cfg.ny, cfg.nz))
+    skw = solver_kwargs(args.mode, tuple(cfg.grid_shape))
     s = AllenCahnSolver(cfg, dtype=pdt, **skw)
     s.set_solid(solid, frac)
     s.init_fields(C, u)
     for _ in range(W):
         s.step()
-    if args.tile:
+    two_d = s.ndim == 2
+    if two_d:
+        tile, tune_ms = (0, 0, 0), 0.0  # 2-D grids: the per-node kernels only
+    elif args.tile:
         s.set_tile(*[int(x) for x in args.tile.split(",")])
         tile, tune_ms = tuple(int(x) for x in args.tile.split(",")), 0.0
     elif not args.no_tune:
@@ -320,21 +335,22 @@ def run_ours(args, rank, world, device):
     if rank == 0:
         peak, peak_kind = peaks()
         f16 = args.precision == "fp16"
-        b_step = B_ALG_STEP[args.precision]
+        b_step = B_ALG_STEP_2D if two_d else B_ALG_STEP[args.precision]
         # the dominant kernel of the step: k_update (two-kernel step) or k_step (fused)
-        kname = "k_update" if two_kernel else "k_step"
-        b_ker = B_ALG_KERNEL[args.precision][kname]
+        kname = ("k2_update" if two_d else "k_update") if two_kernel else "k_step"
+        b_ker = B_ALG_KERNEL_2D[kname] if two_d else B_ALG_KERNEL[args.precision][kname]
         ker_s = upd_ms / K / 1e3
         achieved = b_ker * n / ker_s / 1e9
         traffic_pn = profiled_traffic(kname + ("_f16" if f16 else ""))
         step_bw = b_step * n / (tot_ms / K / 1e3) / 1e9
         kernels = {}
         if two_kernel:
-            b_phi = B_ALG_KERNEL[args.precision]["k_phi"]
-            kernels = {"k_phi": {"ms_per_launch": phi_ms / K, "bytes_per_node": b_phi,
-                                 "achieved_gbs": b_phi * n / (phi_ms / K / 1e3) / 1e9},
-                       "k_update": {"ms_per_launch": upd_ms / K, "bytes_per_node": b_ker,
-                                    "achieved_gbs": achieved}}
+            pname = "k2_phi" if two_d else "k_phi"
+            b_phi = B_ALG_KERNEL_2D[pname] if two_d else B_ALG_KERNEL[args.precision][pname]
+            kernels = {pname: {"ms_per_launch": phi_ms / K, "bytes_per_node": b_phi,
+                               "achieved_gbs": b_phi * n / (phi_ms / K / 1e3) / 1e9},
+                       kname: {"ms_per_launch": upd_ms / K, "bytes_per_node": b_ker,
+                               "achieved_gbs": achieved}}
         w = WORKLOADS[name]
         cpu = None
         if not args.no_cpu_baseline:
@@ -352,8 +368,8 @@ def run_ours(args, rank, world, device):
                        "parallelism": "replicas" if world > 1 else "single",
                        "mode": args.mode,
                        "tile": list(tile), "tuned_ms": tune_ms,
-                       "l2": f"state (f, g: {4 * 19 * n * (2 if f16 else 4) / 1e6:.0f} MB) larger than L2 "
-                             "(129 MB): no flush"},
+                       "l2": f"state (f, g: {4 * s.lattice.q * n * (2 if f16 else 4) / 1e6:.0f} MB) larger "
+                             "than L2 (129 MB): no flush"},
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
                     "d2h_bytes_per_step": d2h / K,
                     "what": f"AllenCahnSolver from host arrays: create + set_solid + init_fields + {K} steps "
@@ -368,8 +384,8 @@ def run_ours(args, rank, world, device):
             "step_roofline": {"achieved_gbs": step_bw, "bytes_per_node": b_step, "peak": peak,
                               "frac": step_bw / peak, "mlups_roofline": peak * 1e3 / b_step},
             "kernels": kernels,
-            # two kernels per step (three with the chemical-potential pass of the grad-mu modes)
-            "gpu_launches": ((3 if args.mode in ("cahn-hilliard", "mu-drive") else 2) * K) if two_kernel else K,
+            # two kernels per step (four with the mu and grad-mu passes of the grad-mu modes)
+            "gpu_launches": ((4 if args.mode in ("cahn-hilliard", "mu-drive") else 2) * K) if two_kernel else K,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "spread_after": {k2: meas[k2] for k2 in ("Dx", "Dy", "k", "z_com", "volume")},

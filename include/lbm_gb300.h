@@ -14,6 +14,9 @@
  * (pytorch-lbm, file:line cited per function).  Layout of every field is the
  * reference's: C-contiguous (nx, ny, nz), z fastest; vectors (3, nx, ny, nz);
  * populations (19, nx, ny, nz) in the D3Q19 order of lbm/lattice.py:70-81.
+ * A grid with nz == 1 is 2-D, as in the reference (lbm/fe_config.py:157):
+ * D2Q9 populations (9, nx, ny) in the order of lbm/lattice.py:46-55, vectors
+ * (2, nx, ny), wall normals (2, nx, ny); "N" below is nx*ny*nz either way.
  */
 #ifndef LBM_GB300_H
 #define LBM_GB300_H
@@ -92,7 +95,10 @@ typedef struct LbmHandle LbmHandle;
 
 /* Allocate the device state of one nx*ny*nz grid on the current CUDA device.
  * Replaces AllenCahnSolver.__init__ (lbm/fe_ac_solver.py:54-191).
- * Only 3-D grids (nz > 1) are supported.  The interface sources that need
+ * nz == 1 makes a 2-D D2Q9 grid (the reference's 2-D path): LBM_F32 or
+ * LBM_F64 only, stepped by its own per-node kernels (no fused tiles, no
+ * autotuning, no batches, no droplet injection: LBM_E_UNSUPPORTED).  3-D
+ * grids need every extent >= 2.  The interface sources that need
  * the gradient of the chemical potential (interface_mode Cahn-Hilliard,
  * mu_drive > 0) add a chemical-potential pass to every step, run on LBM_F32
  * and LBM_F64 grids (LBM_E_UNSUPPORTED with LBM_F16), with the two-kernel
@@ -126,7 +132,7 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction,
 int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype);
 
 /* Initial phase field phi (N elements) and optional velocity u (3N elements,
- * NULL = zero), of element type src_dtype, in host memory (on_device = 0) or
+ * 2N on a 2-D grid; NULL = zero), of element type src_dtype, in host memory (on_device = 0) or
  * device memory (on_device = 1).  Sets f = f_eq(phi, u), g = g_eq(0, u) and
  * the phi-mass reference.  Replaces AllenCahnSolver.init_fields
  * (lbm/fe_ac_solver.py:239-261).  Asynchronous on `stream`. */
@@ -172,7 +178,7 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
 int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u,
                    void* P, void* p, void* mu, void* stream);
 
-/* Current populations f, g (19N each, caller device buffers of the handle's
+/* Current populations f, g (19N each, 9N on a 2-D grid; caller device buffers of the handle's
  * compute type) as the reference holds them between steps (AllenCahnSolver.f/.g,
  * lbm/fe_ac_solver.py:97-98). */
 int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream);
@@ -193,7 +199,7 @@ int lbm_inject_droplet(LbmHandle* h, const double* center3, double radius, doubl
                        int64_t* core_nodes, void* stream);
 
 /* Geometry tables as computed by lbm_set_geometry, into host buffers (any may
- * be NULL): node class byte (N), is_boundary (N), wall_normal (3N float32),
+ * be NULL): node class byte (N), is_boundary (N), wall_normal (3N float32, 2N on a 2-D grid),
  * wall_weight (N float32), near_wall mask (N), partial mask (N).  Mirrors
  * ConningtonLeeWetting.is_boundary / wall_normal / wall_weight /
  * near_wall_mask (lbm/fe_wetting.py:140,147,305-306) and
@@ -221,7 +227,8 @@ int lbm_get_scalars(LbmHandle* h, double* phi_mass_init, double* last_sum_phi,
  * phi with solid zeroed, out[1] C_max, out[2..4] Dx, Dy, Dz extents of the
  * phi > 0.5 fluid set, out[5] k = Dx/Dy, out[6] z centre of mass of that set,
  * out[7] its node count, out[8] 1 if phi has a NaN else 0.  Host output,
- * synchronises `stream`.  Replaces measure_spread_factor
+ * synchronises `stream`.  On a 2-D grid Dz = 0 (as the reference reports for
+ * 2-D fields) and out[6] is the centre along y.  Replaces measure_spread_factor
  * (lbm/fe_measure.py:11-82) and the every-50-steps extent/z_com/NaN check of
  * scripts/run_thesis_sweep.py:182-216. */
 int lbm_measure(LbmHandle* h, double* out9, void* stream);
@@ -230,7 +237,8 @@ int lbm_measure(LbmHandle* h, double* out9, void* stream);
  * phi (solid nodes zeroed), total momentum sum rho(phi) u with rho = phi rho_l
  * + (1 - phi) rho_g, the first and last x, y, z index of the phi > 0.5 set
  * (extents6 = xmin, xmax, ymin, ymax, zmin, zmax; all -1 when the set is
- * empty) and the maximum of phi.  Host outputs (any may be NULL); synchronises
+ * empty) and the maximum of phi.  On a 2-D grid the z momentum is 0 and the
+ * z extents are 0 (-1 when empty).  Host outputs (any may be NULL); synchronises
  * `stream`.  The mass/momentum guard of a solve and the data behind
  * measure_spread_factor (lbm/fe_measure.py:11-82). */
 int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, float* cmax, void* stream);

@@ -201,9 +201,11 @@ __device__ __forceinline__ T edot(int q, T a0, T a1) {
   return T(0);
 }
 
-// Block total published, last block adds the block totals in block order and
-// returns true in thread 0 with the grid total (exact for float phi: unsigned
-// 64-bit fixed point with 31 fraction bits; NaN carried by a flag).
+// Block total published; the last block to finish adds the block totals
+// (each of its threads a fixed strided subset, then a fixed shuffle tree, so
+// the float64 total is the same on every run) and returns true in thread 0
+// with the grid total (exact for float phi: unsigned 64-bit fixed point with
+// 31 fraction bits; NaN carried by a flag).
 constexpr unsigned long long kNaN = ~0ull;
 template <typename T>
 __device__ __forceinline__ bool grid_total(double part_d, unsigned long long part_u, bool nan, double* partials,
@@ -236,24 +238,40 @@ __device__ __forceinline__ bool grid_total(double part_d, unsigned long long par
     s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (!s_last || threadIdx.x != 0) return false;
+  if (!s_last) return false;
   __threadfence();
-  if (sizeof(T) == 8) {
-    const volatile double* p = partials;
-    double t = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) t += p[b];
-    *total = t;
-  } else {
-    const volatile unsigned long long* p = reinterpret_cast<unsigned long long*>(partials);
-    unsigned long long t = 0ull;
-    bool nn = false;
-    for (unsigned b = 0; b < gridDim.x; ++b) {
-      const unsigned long long v = p[b];
+  double td = 0.0;
+  unsigned long long tu = 0ull;
+  bool nn = false;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock) {
+    if (sizeof(T) == 8) {
+      td += ((const volatile double*)partials)[b];
+    } else {
+      const unsigned long long v = ((const volatile unsigned long long*)partials)[b];
       if (v == kNaN) nn = true;
-      else t += v;
+      else tu += v;
     }
-    *total = nn ? __longlong_as_double(0x7ff8000000000000ll) : (double)t / 2147483648.0;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    td += __shfl_down_sync(0xffffffffu, td, o);
+    tu += __shfl_down_sync(0xffffffffu, tu, o);
+  }
+  nn = __syncthreads_or(nn) != 0;
+  if (lane == 0) {
+    su[wid] = tu;
+    sd[wid] = td;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return false;
+  double d = 0.0;
+  unsigned long long r = 0ull;
+  for (int i = 0; i < kBlock / 32; ++i) {
+    r += su[i];
+    d += sd[i];
+  }
+  if (sizeof(T) == 8) *total = d;
+  else *total = nn ? __longlong_as_double(0x7ff8000000000000ll) : (double)r / 2147483648.0;
   *counter = 0u;
   return true;
 }
