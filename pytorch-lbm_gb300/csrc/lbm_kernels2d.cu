@@ -201,6 +201,22 @@ __device__ __forceinline__ T edot(int q, T a0, T a1) {
   return T(0);
 }
 
+// t[q] = (c e_q . (a0, a1)) / d for every q, with one division per opposite
+// pair (q, opp q): e_opp(q) . a = -(e_q . a) exactly, and (c (-x)) / d =
+// -((c x) / d) in IEEE arithmetic, so the opposite's value is the negation.
+// c and d depend on the weight class (cw: per q); the rest value is
+// (c 0) / d.  Same values as the per-q expression of the reference.
+template <typename T, typename CW>
+__device__ __forceinline__ void pair_div(T (&t)[Q9], T a0, T a1, CW cw, T d) {
+  t[0] = (cw(0) * edot(0, a0, a1)) / d;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int q = i < 2 ? 1 + 2 * i : 5 + (i - 2);  // 1, 3, 5, 6
+    t[q] = (cw(q) * edot(q, a0, a1)) / d;
+    t[opp(q)] = -t[q];
+  }
+}
+
 // Block total published; the last block to finish adds the block totals
 // (each of its threads a fixed strided subset, then a fixed shuffle tree, so
 // the float64 total is the same on every run) and returns true in thread 0
@@ -455,9 +471,11 @@ __global__ void __launch_bounds__(kBlock) k2_update(Consts<T> k, State<T, T> s, 
   {
     const T usq = uo0 * uo0 + uo1 * uo1;
     const T b = usq / (T(2) * cs2<T>());
+    T ecs[Q9];
+    pair_div(ecs, uo0, uo1, [](int) { return T(1); }, cs2<T>());
 #pragma unroll
     for (int q = 1; q < Q9; ++q) {
-      const T ec = edot(q, uo0, uo1) / cs2<T>();
+      const T ec = ecs[q];
       const T geq = P * w<T>(q) + w<T>(q) * ((ec + ec * ec / T(2)) - b);
       const T d = g[q] - geq;
       if (ex(q) != 0) sxx = sxx + d;
@@ -545,16 +563,18 @@ __global__ void __launch_bounds__(kBlock) k2_update(Consts<T> k, State<T, T> s, 
   const T usq = u0 * u0 + u1 * u1;
   const T b = usq / (T(2) * cs2<T>());
   const T acT = (T)ac;
+  T ecs[Q9], src[Q9], G[Q9];
+  pair_div(ecs, u0, u1, [](int) { return T(1); }, cs2<T>());
+  pair_div(src, S0, S1, [&](int q) { return acT * w<T>(q); }, cs2<T>());
+  pair_div(G, F0, F1, [&](int q) { return ns * w<T>(q); }, rho_eff * cs2<T>());
 #pragma unroll
   for (int q = 0; q < Q9; ++q) {
-    const T ec = edot(q, u0, u1) / cs2<T>();
+    const T ec = ecs[q];
     const T sq = ec * ec / T(2);
     const T feq = phi * (w<T>(q) * (((T(1) + ec) + sq) - b));
-    const T src = ((acT * w<T>(q)) * edot(q, S0, S1)) / cs2<T>();
-    s.fout[q * Np + n] = (f[q] - k.omega_f * (f[q] - feq)) + src;
+    s.fout[q * Np + n] = (f[q] - k.omega_f * (f[q] - feq)) + src[q];
     const T geq = P * w<T>(q) + w<T>(q) * ((ec + sq) - b);
-    const T G = ((ns * w<T>(q)) * edot(q, F0, F1)) / (rho_eff * cs2<T>());
-    s.gout[q * Np + n] = (g[q] - om * (g[q] - geq)) + G;
+    s.gout[q * Np + n] = (g[q] - om * (g[q] - geq)) + G[q];
   }
   s.u[n] = u0;
   s.u[Np + n] = u1;
