@@ -97,3 +97,67 @@ def test_flat_surface_symmetry():
         s.run(50)
         m = s.measure()
         assert m["Dx"] == m["Dy"] and m["k"] == 1.0, m
+
+
+def _sweep_ridge_case(amp, dtype, n=150):
+    """The sweep driver's ridge case (scripts/run_thesis_sweep.py:36-43, 57-160):
+    D0 = 45, R* = 1, We = 7.9, theta = 162, tau = 0.53, tau_h = 0.57,
+    boundary_relax = 0, geometric wetting on when alpha > 0, 150 x 150 x 107,
+    droplet 2 lattice units above the ridge top, U0 = -0.05."""
+    from geometry.substrate import create_substrate_with_fraction
+    from lbm.fe_ac_solver import AllenCahnSolver
+    from lbm.fe_config import FEConfig
+    from lbm.fe_droplet import create_fe_droplet_with_impact
+    D0, U0, xi, tau = 45.0, -0.05, 4.0, 0.53
+    R = D0 / 2.0
+    sigma = U0 ** 2 * D0 / 7.9
+    beta = 12.0 * sigma / xi
+    nz = min(int(R + 2 + R + 2 * R + 15), 300)
+    cfg = FEConfig(nx=n, ny=n, nz=nz, rho_l=1.0, rho_g=1.0 / 828.0, sigma=sigma, xi=xi, beta=beta,
+                   kappa=beta * xi ** 2 / 8.0, M=0.02 / beta, tau_l=tau, tau_g=tau, tau_h=tau + 0.04,
+                   theta_eq=162.0, device="cuda", g_force=(0.0, 0.0, 0.0))
+    s = AllenCahnSolver(cfg, dtype=dtype, stab_mode="fakhari", boundary_relax=0.0, geometric_wetting=(amp > 0),
+                        geo_amplification=amp)
+    solid, frac = create_substrate_with_fraction(n, n, nz, "ridge", R_star=1.0, R_d=R)
+    s.set_solid(solid, frac)
+    top = int(np.flatnonzero(solid[n // 2, n // 2])[-1])
+    cz = min(top + 2.0 + R, nz - R - 2)
+    C, _, u = create_fe_droplet_with_impact(n, n, nz, center=(n / 2.0, n / 2.0, cz), radius=R, xi=xi,
+                                            u_impact=(0.0, 0.0, U0))
+    s.init_fields(C, u)
+    return s
+
+
+# k_max against alpha_geo of the reference's paper (paper_pof/sections/4_experiments.tex:70-77):
+# ridge R* = 1, We = 7.9, theta = 162, N = 150; alpha 1.0 gives the value of 0.5 (alpha <= 1 is
+# not amplified)
+PAPER_KMAX = {0.0: 1.541, 0.5: 2.290, 1.5: 2.655, 2.0: 4.556}
+
+
+@pytest.mark.parametrize("amp,dtype", [(0.0, torch.float32), (0.5, torch.float32), (1.5, torch.float32),
+                                       (2.0, torch.float32), (1.5, torch.float64)])
+def test_paper_kmax_table(amp, dtype):
+    """The paper's primary result: the maximum spread ratio k = Dx / Dy over a
+    3000-step impact, sampled every 50 steps as the sweep driver does
+    (scripts/run_thesis_sweep.py:182-211), to the paper's three decimals."""
+    s = _sweep_ridge_case(amp, dtype)
+    kmax = 0.0
+    for _ in range(60):
+        s.run(50)
+        kmax = max(kmax, s.measure()["k"])
+    assert round(kmax, 3) == PAPER_KMAX[amp]
+
+
+# grid convergence of k_max at alpha_geo = 1.5 (paper_pof/sections/4_experiments.tex:140-146):
+# the sweep driver's case on n x n x 107 grids
+PAPER_KMAX_GRID = {80: 2.355, 100: 2.586, 120: 2.586, 180: 2.655}
+
+
+@pytest.mark.parametrize("n", sorted(PAPER_KMAX_GRID))
+def test_paper_grid_convergence(n):
+    s = _sweep_ridge_case(1.5, torch.float32, n=n)
+    kmax = 0.0
+    for _ in range(60):
+        s.run(50)
+        kmax = max(kmax, s.measure()["k"])
+    assert round(kmax, 3) == PAPER_KMAX_GRID[n]
