@@ -419,7 +419,11 @@ __global__ void __launch_bounds__(kBlock) k2_gradmu(Consts<T> k, State<T, T> s) 
 // correction; pressure, non-equilibrium stress (new P, old u), forces,
 // velocity, Allen-Cahn source, both BGK collisions; writes fout, gout, u.
 // ac: the python-double Allen-Cahn source coefficient 1 - 1 / (2 tau_f).
-template <typename T, bool RAW, bool FIRST, bool GMU>
+// OMEGA1: tau_f == 1 (the reference's default tau_h), where the phase-field
+// collision f - (f - f_eq) + src is taken as f_eq + src and f is not read
+// again (the two differ by at most an ulp of f where f and f_eq are more
+// than a factor of two apart).
+template <typename T, bool RAW, bool FIRST, bool GMU, bool OMEGA1 = false>
 __global__ void __launch_bounds__(kBlock) k2_update(Consts<T> k, State<T, T> s, double ac) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
   if (n >= k.N) return;
@@ -550,7 +554,7 @@ __global__ void __launch_bounds__(kBlock) k2_update(Consts<T> k, State<T, T> s, 
 
   // 8. collisions (:496-530); the pre-collision f is this step's pulled f
   T f[Q9];
-  fetch_f9<T, RAW>(f, k, s, n, nb, c, eps);
+  if (!OMEGA1) fetch_f9<T, RAW>(f, k, s, n, nb, c, eps);
   T om, ns;
   if (k.tau_const) {
     om = k.omega_g;
@@ -572,7 +576,7 @@ __global__ void __launch_bounds__(kBlock) k2_update(Consts<T> k, State<T, T> s, 
     const T ec = ecs[q];
     const T sq = ec * ec / T(2);
     const T feq = phi * (w<T>(q) * (((T(1) + ec) + sq) - b));
-    s.fout[q * Np + n] = (f[q] - k.omega_f * (f[q] - feq)) + src[q];
+    s.fout[q * Np + n] = OMEGA1 ? feq + src[q] : (f[q] - k.omega_f * (f[q] - feq)) + src[q];
     const T geq = P * w<T>(q) + w<T>(q) * ((ec + sq) - b);
     s.gout[q * Np + n] = (g[q] - om * (g[q] - geq)) + G[q];
   }
@@ -690,6 +694,8 @@ cudaError_t launch_step2d(const Consts<T>& k, const State<T, T>& s, bool raw, bo
     LBM_UPD2(true, false)
   } else if (first) {
     LBM_UPD2(false, true)
+  } else if (!gmu && k.omega_f == T(1)) {
+    d2::k2_update<T, false, false, false, true><<<nb, kBlock, 0, st>>>(k, s, ac);
   } else {
     LBM_UPD2(false, false)
   }
