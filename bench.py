@@ -538,14 +538,20 @@ def run_serve(args, device):
             for i, a in enumerate(arr)]
     budget = int(args.serve_budget_gb * 1e9)
     res_b, st_b = serve(reqs, GpuBackend(torch.float16), budget, tick=100, builders=4)
+    # shortest remaining work first, at least args.serve_saturate nodes per tick
+    res_r, st_r = serve(reqs, GpuBackend(torch.float16), budget, tick=100, builders=4,
+                        saturate_nodes=int(args.serve_saturate))
     res_s, st_s = serve_sequential(reqs, GpuBackend(torch.float32))
     return {"metric": "MLUPS", "value": st_b["mlups"], "unit": "MLUPS", "n_gpus": 1, "higher_is_better": True,
             "dtype": "f16 storage / f32 math", "data": "synthetic",
             "config": {"workload": f"serving: {len(reqs)} impact requests, Poisson 4/s, grids up to 256x256x192, "
                                    f"steps U[1000,4000], HBM budget {args.serve_budget_gb} GB",
                        "node_updates": float(sum(r.case.nodes * r.case.steps for r in reqs))},
-            "served_f16_batched": st_b, "plain_f32_sequential": st_s,
-            "mlups_ratio": st_b["mlups"] / st_s["mlups"], "p99_ratio": st_b["p99_s"] / st_s["p99_s"]}
+            "served_f16_batched": st_b, "served_f16_srpt": dict(st_r, saturate_nodes=int(args.serve_saturate)),
+            "plain_f32_sequential": st_s,
+            "mlups_ratio": st_b["mlups"] / st_s["mlups"], "p99_ratio": st_b["p99_s"] / st_s["p99_s"],
+            "srpt_mlups_ratio": st_r["mlups"] / st_s["mlups"], "srpt_p50_ratio": st_r["p50_s"] / st_s["p50_s"],
+            "srpt_p99_ratio": st_r["p99_s"] / st_s["p99_s"]}
 
 
 def barrier(world):
@@ -585,6 +591,8 @@ def main():
     ap.add_argument("--precision-every", type=int, default=500, help="measurement interval of that solve")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-saturate", type=float, default=4e6,
+                    help="nodes per tick of the shortest-remaining-work-first serving policy")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")

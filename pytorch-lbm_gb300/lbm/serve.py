@@ -100,13 +100,35 @@ def _stats(results, wall):
             "mlups": updates / wall / 1e6 if wall > 0 else 0.0}
 
 
-def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0, clock=time.perf_counter,
-          sleep=time.sleep):
+def _select(active, saturate_nodes):
+    """Resident cases to step in the next tick.  saturate_nodes None: all of
+    them (processor sharing).  Otherwise shortest remaining work first
+    (nodes x remaining steps, then request id): cases in that order until
+    their nodes reach saturate_nodes, so that the GPU stays busy while the
+    cases closest to completion go first."""
+    keys = sorted(active)
+    if saturate_nodes is None:
+        return tuple(keys)
+    order = sorted(keys, key=lambda k: (active[k][0].case.nodes * active[k][2], k))
+    picked, nodes = [], 0
+    for k in order:
+        picked.append(k)
+        nodes += active[k][0].case.nodes
+        if nodes >= saturate_nodes:
+            break
+    return tuple(sorted(picked))
+
+
+def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0, saturate_nodes=None,
+          clock=time.perf_counter, sleep=time.sleep):
     """Continuous batching of `requests` under an HBM budget and at most
     `max_slots` resident cases (None: no limit).  With builders > 0, admitted
     cases are set up (inputs, geometry, init) by that many host threads while
     the GPU keeps stepping the resident ones; their footprint counts against
-    the budget from the start of the set-up.  Returns (results in completion
+    the budget from the start of the set-up.  saturate_nodes (None: every
+    resident case advances in every tick) selects shortest-remaining-work-first
+    ticks that step only the resident cases closest to completion, at least
+    that many nodes of them (see _select).  Returns (results in completion
     order, stats)."""
     from concurrent.futures import ThreadPoolExecutor
     pending = sorted(requests, key=lambda r: r.arrival)
@@ -144,16 +166,17 @@ def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0,
                 else:
                     sleep(max(0.0, pending[0].arrival - (clock() - t0)))  # idle until the next arrival
                 continue
-            key = tuple(sorted(active))
+            key = _select(active, saturate_nodes)
             if key != members:
                 if batch is not None:
                     batch.close()
                 batch = backend.batch([active[k][1] for k in key])
                 members = key
-            n = min(tick, min(a[2] for a in active.values()))
+            n = min(tick, min(active[k][2] for k in key))
             batch.run(n)
             done = []
-            for k, a in active.items():
+            for k in key:
+                a = active[k]
                 a[2] -= n
                 if a[2] == 0:
                     done.append(k)

@@ -30,10 +30,15 @@ def _requests():
     return [Request(i, c, 0.02 * i) for i, c in enumerate(cases)]
 
 
-@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
-def test_served_results_equal_alone(dtype):
+@pytest.mark.parametrize("dtype,saturate", [(torch.float32, None), (torch.float16, None),
+                                             (torch.float16, 30_000)])
+def test_served_results_equal_alone(dtype, saturate):
+    """Processor sharing, and shortest-remaining-work-first ticks (saturate:
+    cases paused while others run), give every request the result it has
+    alone."""
     reqs = _requests()
-    mix, st = serve(reqs, GpuBackend(dtype, keep_phi=True), budget_bytes=2 * 10 ** 9, tick=8)
+    mix, st = serve(reqs, GpuBackend(dtype, keep_phi=True), budget_bytes=2 * 10 ** 9, tick=8,
+                    saturate_nodes=saturate)
     alone, _ = serve_sequential(reqs, GpuBackend(dtype, keep_phi=True))
     assert len(mix) == len(reqs) == len(alone)
     a = {r.rid: r for r in alone}

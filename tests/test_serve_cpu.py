@@ -157,3 +157,38 @@ def test_background_setup_serves_every_request():
     res, st = serve(reqs, be, 10 ** 12, tick=64, builders=2, clock=clk, sleep=clk.sleep)
     assert sorted(r.rid for r in res) == [r.rid for r in reqs]
     assert all(r.measure["steps"] == r.steps for r in res)
+
+
+def test_shortest_remaining_work_first():
+    """saturate_nodes: each tick steps the cases with the least remaining work
+    until their nodes reach the threshold; every request is still served
+    exactly, the GPU time is the same, and short requests finish sooner."""
+    reqs = _requests(n=16, seed=5)
+    c0 = Clock()
+    ps, st_ps = serve(reqs, FakeBackend(c0), budget_bytes=10 ** 12, tick=50, clock=c0, sleep=c0.sleep)
+    c1 = Clock()
+    b1 = FakeBackend(c1)
+    sr, st_sr = serve(reqs, b1, budget_bytes=10 ** 12, tick=50, saturate_nodes=400_000, clock=c1, sleep=c1.sleep)
+    assert sorted(r.rid for r in sr) == list(range(len(reqs)))
+    for r in sr:
+        assert r.measure["steps"] == r.steps
+    assert st_sr["wall_s"] == pytest.approx(st_ps["wall_s"], rel=1e-9)
+    assert st_sr["mean_s"] < st_ps["mean_s"] and st_sr["p50_s"] <= st_ps["p50_s"]
+    # a tick with several resident cases steps only some of them
+    assert any(k < max(kk for _, kk in b1.ticks) for _, k in b1.ticks)
+
+
+def test_select_order():
+    from lbm.serve import _select
+
+    class R:
+        def __init__(self, nodes):
+            self.case = Case((nodes, 1, 1), 0)
+
+    active = {0: [R(100), None, 50], 1: [R(10), None, 100], 2: [R(1000), None, 1], 3: [R(10), None, 10]}
+    # remaining work: 0 -> 5000, 1 -> 1000, 2 -> 1000, 3 -> 100
+    assert _select(active, None) == (0, 1, 2, 3)
+    assert _select(active, 5) == (3,)
+    assert _select(active, 15) == (1, 3)
+    assert _select(active, 1015) == (1, 2, 3)
+    assert _select(active, 10 ** 9) == (0, 1, 2, 3)
