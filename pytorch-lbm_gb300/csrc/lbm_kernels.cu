@@ -1028,9 +1028,8 @@ __device__ __forceinline__ void decode(const FastDiv& dz, const FastDiv& dy, int
 // per-block publication of the partial sum happens once per block.
 // phi of node n (written to phi_out) added to the block's sum.
 template <typename T, typename S, bool RAW>
-__device__ __forceinline__ void phi_node(const Consts<T>& k, const State<T, S>& s, int n, const Pol& pol,
+__device__ __forceinline__ void phi_node(const Consts<T>& k, const State<T, S>& s, int n, uint8_t c, const Pol& pol,
                                          TileSum<T>& part) {
-  const uint8_t c = s.cls[n];
   T phi = T(0);
   if (!(c & kSolid)) {
     int ix, iy, iz;
@@ -1070,7 +1069,8 @@ template <typename T, typename S, bool RAW>
 __global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
   const Pol pol = Pol::make();
   TileSum<T> part;
-  for (int n = blockIdx.x * kBlock + threadIdx.x; n < k.N; n += gridDim.x * kBlock) phi_node<T, S, RAW>(k, s, n, pol, part);
+  for (int n = blockIdx.x * kBlock + threadIdx.x; n < k.N; n += gridDim.x * kBlock)
+    phi_node<T, S, RAW>(k, s, n, s.cls[n], pol, part);
   phi_finish(s, part, blockIdx.x, gridDim.x);
 }
 
@@ -1197,7 +1197,16 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) k_phi_batch(co
   const Pol pol = Pol::make();
   const int b = blockIdx.x - d.phi_blk0, nb = d.phi_nblk;
   TileSum<T> part;
-  for (int n = b * kBlock + threadIdx.x; n < d.k.N; n += nb * kBlock) phi_node<T, S, false>(d.k, d.s, n, pol, part);
+  // the class byte of the thread's next node is loaded one node ahead, so
+  // that the pulled loads of a node do not wait for its class load
+  const int N = d.k.N, stride = nb * kBlock;
+  int n = b * kBlock + threadIdx.x;
+  uint8_t c = n < N ? d.s.cls[n] : 0;
+  for (; n < N; n += stride) {
+    const uint8_t c_next = n + stride < N ? d.s.cls[n + stride] : 0;
+    phi_node<T, S, false>(d.k, d.s, n, c, pol, part);
+    c = c_next;
+  }
   phi_finish(d.s, part, b, nb);
 }
 
