@@ -97,7 +97,7 @@ typedef struct LbmHandle LbmHandle;
  * Replaces AllenCahnSolver.__init__ (lbm/fe_ac_solver.py:54-191).
  * nz == 1 makes a 2-D D2Q9 grid (the reference's 2-D path): LBM_F32 or
  * LBM_F64 only, stepped by its own per-node kernels (no fused tiles, no
- * autotuning, no batches, no droplet injection: LBM_E_UNSUPPORTED).  3-D
+ * autotuning, no batches: LBM_E_UNSUPPORTED).  3-D
  * grids need every extent >= 2.  The interface sources that need
  * the gradient of the chemical potential (interface_mode Cahn-Hilliard,
  * mu_drive > 0) add a chemical-potential pass to every step, run on LBM_F32
@@ -184,7 +184,8 @@ int lbm_get_fields(LbmHandle* h, uint32_t mask, void* phi, void* rho, void* u,
 int lbm_get_populations(LbmHandle* h, void* f, void* g, void* stream);
 
 /* Inject a droplet mid-run: centre (3 doubles, lattice units), radius,
- * interface width xi, impact velocity (3 doubles, NULL = zero).  As the
+ * interface width xi, impact velocity (3 doubles, NULL = zero); a 2-D grid
+ * reads the first two components of each.  As the
  * reference: phi becomes max(phi, C) where the droplet profile
  * C = 0.5 + 0.5 tanh(2 (R - |x - centre|) / xi) exceeds 0.1 (its core), u
  * becomes (1 - C) u + C u_impact everywhere, f and g are reset to their

@@ -57,6 +57,9 @@ cudaError_t launch_observe2d(const Consts<T>&, const State<T, T>&, bool, unsigne
                              cudaStream_t);
 template <typename T>
 cudaError_t launch_populations2d(const Consts<T>&, const State<T, T>&, bool, T*, T*, cudaStream_t);
+template <typename T>
+cudaError_t launch_inject2d(const Consts<T>&, const State<T, T>&, bool, const InjectParams&, const T*, unsigned*,
+                            cudaStream_t);
 
 template <typename T, typename S>
 size_t case_desc_bytes();
@@ -942,7 +945,6 @@ int lbm_inject_droplet(LbmHandle* h, const double* center3, double radius, doubl
   if (!h || !center3) return fail(LBM_E_ARG, "lbm_inject_droplet: null argument");
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_inject_droplet: call lbm_init_fields first");
   if (!(radius >= 0.0) || !(xi > 0.0)) return fail(LBM_E_ARG, "lbm_inject_droplet: radius >= 0 and xi > 0 required");
-  if (is2d(h)) return fail(LBM_E_UNSUPPORTED, "lbm_inject_droplet: 3-D grids only");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   InjectParams ip;
   std::memset(&ip, 0, sizeof(ip));
@@ -963,12 +965,25 @@ int lbm_inject_droplet(LbmHandle* h, const double* center3, double radius, doubl
       // the P attribute: the pressure of the last step, into the measure scratch
       State<T, S> so = make_state<T, S>(*h, h->cur ^ 1, h->pc ^ 1);
       so.c_cur = h->c_last;
-      r = launch_observe<T, S>(k, so, h->last_raw_in, LBM_FIELD_P, 1, nullptr, nullptr, nullptr,
-                               static_cast<T*>(h->meas_phi), nullptr, nullptr, st);
+      if constexpr (sizeof(S) == sizeof(T)) {
+        if (is2d(h))
+          r = launch_observe2d<T>(k, so, h->last_raw_in, LBM_FIELD_P, 1, nullptr, nullptr, nullptr,
+                                  static_cast<T*>(h->meas_phi), nullptr, nullptr, st);
+        else
+          r = launch_observe<T, S>(k, so, h->last_raw_in, LBM_FIELD_P, 1, nullptr, nullptr, nullptr,
+                                   static_cast<T*>(h->meas_phi), nullptr, nullptr, st);
+      } else {
+        r = launch_observe<T, S>(k, so, h->last_raw_in, LBM_FIELD_P, 1, nullptr, nullptr, nullptr,
+                                 static_cast<T*>(h->meas_phi), nullptr, nullptr, st);
+      }
       if (r != cudaSuccess) return r;
     }
     State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
     s.c_prev = h->c_last;
+    if constexpr (sizeof(S) == sizeof(T)) {
+      if (is2d(h))
+        return launch_inject2d<T>(k, s, h->raw, ip, static_cast<const T*>(h->meas_phi), h->counters + 3, st);
+    }
     return launch_inject<T, S>(k, s, h->raw, ip, static_cast<const T*>(h->meas_phi), h->counters + 3, st);
   });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_inject_droplet: ") + cudaGetErrorString(e));

@@ -653,6 +653,84 @@ __global__ void __launch_bounds__(kBlock) k2_populations(Consts<T> k, State<T, T
   }
 }
 
+// Mid-run droplet injection (lbm/fe_ac_solver.py:645-732) on a 2-D grid: the
+// 3-D k_inject's steps with D2Q9 and two velocity components.  Reads the
+// state as the reference holds it between steps (phi / u / P attributes,
+// populations as k2_populations rebuilds them), blends the droplet in and
+// writes the raw state init_fields leaves: f, g to the other population
+// buffer, phi to the other phi buffer, u in place.  Sums the new phi (the new
+// phi-mass reference) and counts the core nodes.
+template <typename T, bool RAW>
+__global__ void __launch_bounds__(kBlock) k2_inject(Consts<T> k, State<T, T> s, InjectParams ip,
+                                                    const T* __restrict__ P_attr, unsigned* core_count) {
+  const int n = blockIdx.x * kBlock + threadIdx.x;
+  double part = 0.0;
+  bool core = false;
+  if (n < k.N) {
+    const int Np = k.Np;
+    const uint8_t c = s.cls[n];
+    const Nb2 nb = make_nb2(n, k.nx, k.ny);
+    const int ix = n / k.ny, iy = n - (n / k.ny) * k.ny;
+    // the droplet as the reference builds it: float64 profile, stored as float32
+    const double dx = ix - ip.c[0], dy = iy - ip.c[1];
+    const double dist = sqrt(dx * dx + dy * dy);
+    double Cd = 0.5 + 0.5 * tanh(2.0 * (ip.radius - dist) / ip.xi);
+    Cd = Cd < 0.0 ? 0.0 : (Cd > 1.0 ? 1.0 : Cd);
+    const T C = (T)(float)Cd;
+    core = C > T(0.1);
+    // the attributes phi, u, P the reference holds now
+    const T corr = s.cbuf[s.c_prev];
+    T phi = s.phi_in[n];
+    if (!ip.obs_init) {
+      const T pr = phi;
+      phi = clamp01(pr * corr);
+      if (k.relax_on && (c & kTop)) {
+        const T r = relax_target(k, s.phi_in, s.nsw, s.cubic, n, pr, corr);
+        if (r >= T(0)) phi = r;
+      }
+    }
+    T u0 = s.u[n], u1 = s.u[Np + n];
+    const T P = ip.obs_init ? T(0) : P_attr[n];
+    const T eps = (c & kPartial) ? s.eps[n] : T(0);
+    T fv[Q9], gv[Q9];
+    fetch_f9<T, RAW>(fv, k, s, n, nb, c, eps);
+    fetch9<T, RAW>(gv, s.gin, Np, n, nb, c, eps, T(1));
+    // new phi: the maximum with the droplet in its core, clamped, zero in solid
+    T pn = core ? (phi > C ? phi : C) : phi;
+    pn = clamp01(pn);
+    if (c & kSolid) pn = T(0);
+    // new u: (1 - C) u + C u_impact everywhere, zero in solid
+    u0 = (T(1) - C) * u0 + C * (T)ip.u[0];
+    u1 = (T(1) - C) * u1 + C * (T)ip.u[1];
+    if (c & kSolid) u0 = u1 = T(0);
+    if (core) {
+      const T b = (u0 * u0 + u1 * u1) / (T(2) * cs2<T>());
+#pragma unroll
+      for (int q = 0; q < Q9; ++q) {
+        const T ec = edot(q, u0, u1) / cs2<T>();
+        fv[q] = pn * (w<T>(q) * (((T(1) + ec) + ec * ec / T(2)) - b));
+        gv[q] = P * w<T>(q) + w<T>(q) * ((ec + ec * ec / T(2)) - b);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < Q9; ++q) {
+      s.fout[q * Np + n] = fv[q];
+      s.gout[q * Np + n] = gv[q];
+    }
+    s.u[n] = u0;
+    s.u[Np + n] = u1;
+    s.phi_out[n] = pn;
+    part = (double)pn;
+  }
+  const int cnt = __syncthreads_count(core);
+  if (threadIdx.x == 0 && cnt) atomicAdd(core_count, (unsigned)cnt);
+  double total;
+  if (grid_total<double>(part, 0ull, false, s.partials, s.counter, &total)) {
+    s.scal[0] = (double)(T)total;  // phi_mass_init = phi.sum().item() in T
+    s.scal[1] = total;
+  }
+}
+
 inline int blocks_of(int N) { return (N + kBlock - 1) / kBlock; }
 
 }  // namespace d2
@@ -720,6 +798,15 @@ cudaError_t launch_populations2d(const Consts<T>& k, const State<T, T>& s, bool 
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_inject2d(const Consts<T>& k, const State<T, T>& s, bool raw, const InjectParams& ip,
+                            const T* P_attr, unsigned* core_count, cudaStream_t st) {
+  const int nb = d2::blocks_of(k.N);
+  if (raw) d2::k2_inject<T, true><<<nb, kBlock, 0, st>>>(k, s, ip, P_attr, core_count);
+  else d2::k2_inject<T, false><<<nb, kBlock, 0, st>>>(k, s, ip, P_attr, core_count);
+  return cudaGetLastError();
+}
+
 #define LBM_INST2D(T)                                                                                               \
   template cudaError_t launch_init2d<T, float>(const Consts<T>&, const State<T, T>&, const float*, const float*,    \
                                                cudaStream_t);                                                       \
@@ -729,7 +816,9 @@ cudaError_t launch_populations2d(const Consts<T>& k, const State<T, T>& s, bool 
                                         cudaEvent_t);                                                               \
   template cudaError_t launch_observe2d<T>(const Consts<T>&, const State<T, T>&, bool, unsigned, int, T*, T*, T*,   \
                                            T*, T*, T*, cudaStream_t);                                               \
-  template cudaError_t launch_populations2d<T>(const Consts<T>&, const State<T, T>&, bool, T*, T*, cudaStream_t);
+  template cudaError_t launch_populations2d<T>(const Consts<T>&, const State<T, T>&, bool, T*, T*, cudaStream_t);  \
+  template cudaError_t launch_inject2d<T>(const Consts<T>&, const State<T, T>&, bool, const InjectParams&, const T*, \
+                                          unsigned*, cudaStream_t);
 LBM_INST2D(float)
 LBM_INST2D(double)
 #undef LBM_INST2D

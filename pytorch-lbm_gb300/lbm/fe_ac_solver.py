@@ -20,8 +20,8 @@ the reference holds after the same step.  Each read returns a new tensor.
 the cubic-wall-energy value.  A 2-D grid (``nz == 1``) runs the D2Q9 form
 of the same step (csrc/lbm_kernels2d.cu) in float32 or float64, with fields
 of shape ``(nx, ny)`` and ``u`` of shape ``(2, nx, ny)``, as the reference's
-2-D path; it steps one grid at a time (no batches, no fused tiles, no
-``inject_droplet``).
+2-D path; it steps one grid at a time (no batches, no fused tiles, no half
+storage).
 """
 from __future__ import annotations
 
@@ -300,12 +300,12 @@ class AllenCahnSolver:
         nodes, the phi-mass reference re-based, no previous phi u."""
         if not self._initialized:
             raise RuntimeError("init_fields must be called before inject_droplet()")
-        if self.ndim == 2:
-            raise NotImplementedError("inject_droplet runs on 3-D grids")
         if u_impact is None:
-            u_impact = (0.0,) * 3
-        c = (ctypes.c_double * 3)(*[float(x) for x in center])
-        uv = (ctypes.c_double * 3)(*[float(x) for x in u_impact])
+            u_impact = (0.0,) * self.ndim
+        # the C ABI takes three components; a 2-D grid ignores the third
+        pad = lambda v: [float(x) for x in v][:3] + [0.0] * (3 - min(len(v), 3))
+        c = (ctypes.c_double * 3)(*pad(center))
+        uv = (ctypes.c_double * 3)(*pad(u_impact))
         core = ctypes.c_int64()
         nat.check(self._lib.lbm_inject_droplet(self._h, c, float(radius), float(xi), uv, ctypes.byref(core),
                                                nat.stream_ptr()), "lbm_inject_droplet")

@@ -100,8 +100,6 @@ def test_refused_options():
     with pytest.raises(NotImplementedError):
         AllenCahnSolver(config(case, "cuda"), dtype=torch.float16)
     s = _solver("flat2d_q120")
-    with pytest.raises(NotImplementedError):
-        s.inject_droplet((24, 20), 5.0, 4.0)
     with pytest.raises(RuntimeError, match="2-D"):
         s.set_tile(4, 4, 4)
     with pytest.raises(RuntimeError, match="2-D"):

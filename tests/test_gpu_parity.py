@@ -183,8 +183,9 @@ def test_autotune_leaves_state_unchanged():
         assert (a.phi - b.phi).abs().max().item() <= 2e-6
 
 
+@pytest.mark.parametrize("dim", [3, 2])
 @pytest.mark.parametrize("dn", ["float32", "float64"])
-def test_inject_droplet_vs_reference_and_oracle(dn):
+def test_inject_droplet_vs_reference_and_oracle(dn, dim):
     """Mid-run droplet injection (lbm/fe_ac_solver.py:645-732) on the GPU
     against the reference's own outputs (tests/golden/make_golden_inject.py)
     and the oracle: fields and populations right after the injection, then
@@ -193,9 +194,10 @@ def test_inject_droplet_vs_reference_and_oracle(dn):
     sharpening direction there is set by rounding)."""
     import os
     from lbm.fe_ac_solver import AllenCahnSolver
-    from make_golden_inject import INJECT_CASE as case
+    from make_golden_inject import INJECT_CASE, INJECT_CASE_2D
     from _cases import GOLDEN
-    gd = np.load(os.path.join(GOLDEN, f"inject_ridge_{dn}.npz"))
+    case = INJECT_CASE if dim == 3 else INJECT_CASE_2D
+    gd = np.load(os.path.join(GOLDEN, f"inject_ridge{'' if dim == 3 else '2d'}_{dn}.npz"))
     solid, frac, C, u = inputs(case)
     s = AllenCahnSolver(config(case, "cuda"), dtype=getattr(torch, dn), **case["kw"])
     s.set_solid(solid, frac)

@@ -77,14 +77,17 @@ def test_long_runs_match_reference(name):
     np.testing.assert_allclose(masses, gd["mass_every"], rtol=1e-6)
 
 
+@pytest.mark.parametrize("dim", [3, 2])
 @pytest.mark.parametrize("dn", ["float32", "float64"])
-def test_inject_droplet_matches_reference(dn):
+def test_inject_droplet_matches_reference(dn, dim):
     """Mid-run droplet injection (lbm/fe_ac_solver.py:645-732) against the
-    reference's own outputs (tests/golden/make_golden_inject.py)."""
+    reference's own outputs (tests/golden/make_golden_inject.py), on a 3-D
+    and a 2-D grid."""
     import os
-    from make_golden_inject import INJECT_CASE as case
+    from make_golden_inject import INJECT_CASE, INJECT_CASE_2D
     from _cases import GOLDEN
-    gd = np.load(os.path.join(GOLDEN, f"inject_ridge_{dn}.npz"))
+    case = INJECT_CASE if dim == 3 else INJECT_CASE_2D
+    gd = np.load(os.path.join(GOLDEN, f"inject_ridge{'' if dim == 3 else '2d'}_{dn}.npz"))
     solid, frac, C, u = inputs(case)
     s = OracleSolver(config(case), dtype=np.dtype(dn), **case["kw"])
     s.set_solid(solid, frac)
