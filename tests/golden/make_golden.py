@@ -32,6 +32,8 @@ def alpha_ramp(grid, lo, hi):
     scripts/adaptive_alpha_study.py:157-160."""
     nx, ny, nz = grid
     ramp = (np.float32(lo) + np.float32(hi - lo) * np.arange(nx, dtype=np.float32) / np.float32(nx - 1))
+    if nz == 1:  # a 2-D grid
+        return np.ascontiguousarray(np.broadcast_to(ramp[:, None], (nx, ny)), dtype=np.float32)
     return np.ascontiguousarray(np.broadcast_to(ramp[:, None, None], (nx, ny, nz)), dtype=np.float32)
 
 
@@ -117,6 +119,10 @@ CASES = {
     "direct2d_l150": dict(
         grid=(64, 48, 1), substrate=("fraction", "ridge", 1.0, 8.0), drop=dict(center=(32, 15), radius=8.0, u=(0, -0.05)),
         cfg=dict(theta_eq=150.0), kw=dict(direct_wetting=True, mu_drive=0.5, geo_amplification=1.5, geometric_wetting=True),
+        dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
+    "ridge2d_alpha_field": dict(
+        grid=(64, 48, 1), substrate=("fraction", "ridge", 1.0, 8.0), drop=dict(center=(32, 19), radius=8.0, u=(0, -0.05)),
+        cfg=dict(theta_eq=162.0), kw=dict(geo_amplification=alpha_ramp((64, 48, 1), 0.6, 2.4), geometric_wetting=True),
         dtypes=("float32", "float64"), ckpt=(1, 5), save_f=False),
     "ridge2d_long": dict(
         grid=(128, 64, 1), substrate=("fraction", "ridge", 1.0, 8.0), drop=dict(center=(64, 19), radius=8.0, u=(0, -0.05)),
