@@ -99,12 +99,13 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
   const int nq = two_d ? kQ2 : kQ;
   const int(*E)[3] = two_d ? kE2 : kE;
   g.solid.assign(N, 0);
-  for (int64_t n = 0; n < N; ++n) g.solid[n] = solid_in[n] ? 1 : 0;
   g.partial.assign(N, 0);
   g.fraction.assign(0, 0.0);
-  if (fraction_dtype != 0) {
-    g.fraction.resize(N);
-    for (int64_t n = 0; n < N; ++n) {
+  if (fraction_dtype != 0) g.fraction.resize(N);
+  parallel_for(N, [&](int64_t n0, int64_t n1) {
+    for (int64_t n = n0; n < n1; ++n) {
+      g.solid[n] = solid_in[n] ? 1 : 0;
+      if (fraction_dtype == 0) continue;
       bool part;
       if (fraction_dtype == 1) {
         const float v = static_cast<const float*>(fraction)[n];
@@ -117,7 +118,7 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
       }
       g.partial[n] = (part && !g.solid[n]) ? 1 : 0;
     }
-  }
+  });
   g.boundary.assign(N, 0);
   g.near_wall.assign(N, 0);
   g.top.assign(N, 0);
@@ -128,17 +129,22 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
 
   if (wetting) {
     // boundary: fluid node whose periodic neighbour x - e_q is solid for some
-    // q, found from the solid side: every fluid x = m + e_q of a solid m
-    // (solid nodes are the smaller set)
-    for (int64_t ix = 0; ix < nx; ++ix)
-      for (int64_t iy = 0; iy < ny; ++iy)
-        for (int64_t iz = 0; iz < nz; ++iz) {
-          if (!g.solid[idx(ix, iy, iz, ny, nz)]) continue;
-          for (int q = 1; q < nq; ++q) {
-            const int64_t n = idx(wrap(ix + E[q][0], nx), wrap(iy + E[q][1], ny), wrap(iz + E[q][2], nz), ny, nz);
-            if (!g.solid[n]) g.boundary[n] = 1;
+    // q, found from the solid side (solid nodes are the smaller set): every
+    // fluid x = m + e_q of a solid m.  Threads take slabs of x; a target in a
+    // neighbouring slab may be marked by two threads, so the marks are relaxed
+    // atomic stores of the same value.
+    parallel_for(nx, [&](int64_t x0, int64_t x1) {
+      for (int64_t ix = x0; ix < x1; ++ix)
+        for (int64_t iy = 0; iy < ny; ++iy)
+          for (int64_t iz = 0; iz < nz; ++iz) {
+            if (!g.solid[idx(ix, iy, iz, ny, nz)]) continue;
+            for (int q = 1; q < nq; ++q) {
+              const int64_t n =
+                  idx(wrap(ix + E[q][0], nx), wrap(iy + E[q][1], ny), wrap(iz + E[q][2], nz), ny, nz);
+              if (!g.solid[n]) __atomic_store_n(&g.boundary[n], (uint8_t)1, __ATOMIC_RELAXED);
+            }
           }
-        }
+    });
     for (int64_t n = 0; n < N; ++n) g.n_boundary += g.boundary[n];
     // wall normals
     if (fraction_dtype == 1) {
@@ -146,8 +152,9 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
     } else if (fraction_dtype == 2) {
       smooth_normals(static_cast<const double*>(fraction), g.boundary, nx, ny, nz, g.wall_normal);
     } else {
-      // discrete neighbour counting with non-periodic bounds (fe_wetting.py:152-178)
-      for (int64_t ix = 0; ix < nx; ++ix)
+      // discrete neighbour counting with non-periodic bounds (fe_wetting.py:152-203)
+      parallel_for(nx, [&](int64_t x0, int64_t x1) {
+      for (int64_t ix = x0; ix < x1; ++ix)
         for (int64_t iy = 0; iy < ny; ++iy)
           for (int64_t iz = 0; iz < nz; ++iz) {
             const int64_t n = idx(ix, iy, iz, ny, nz);
@@ -172,6 +179,7 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
             }
             for (int d = 0; d < 3; ++d) g.wall_normal[d * N + n] = (float)nm[d];
           }
+      });
     }
     // Near-wall distance: 11 synchronous passes of periodic face-neighbour
     // min-plus from the boundary nodes (fe_wetting.py:280-292) equal the
@@ -201,19 +209,22 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
     // wall weight exp(-dist / (xi/2)) in float32, 0 in solid (fe_wetting.py:295-303)
     float lut[kWwCodes];
     near_wall_weights(lut);
-    for (int64_t n = 0; n < N; ++n) {
-      if (g.solid[n]) {
-        g.dist[n] = 100;
-        g.wall_weight[n] = 0.0f;
-      } else {
-        g.wall_weight[n] = lut[g.dist[n] <= kNearWallPasses ? g.dist[n] : kWwFarCode];
-        g.near_wall[n] = g.dist[n] < 10 ? 1 : 0;  // dist < 2 xi
+    parallel_for(N, [&](int64_t n0, int64_t n1) {
+      for (int64_t n = n0; n < n1; ++n) {
+        if (g.solid[n]) {
+          g.dist[n] = 100;
+          g.wall_weight[n] = 0.0f;
+        } else {
+          g.wall_weight[n] = lut[g.dist[n] <= kNearWallPasses ? g.dist[n] : kWwFarCode];
+          g.near_wall[n] = g.dist[n] < 10 ? 1 : 0;  // dist < 2 xi
+        }
       }
-    }
+    });
     // top-surface flag of the boundary-phi relaxation, |n_last| / |n| > 1/2
     // in the solver precision, n_last the component along the last axis (z,
     // or y on a 2-D grid) (fe_ac_solver.py:602-606)
-    for (int64_t n = 0; n < N; ++n) {
+    parallel_for(N, [&](int64_t n0, int64_t n1) {
+    for (int64_t n = n0; n < n1; ++n) {
       if (!g.boundary[n]) continue;
       const float a = g.wall_normal[n], b = g.wall_normal[N + n], c = g.wall_normal[2 * N + n];
       bool top;
@@ -240,12 +251,14 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
       }
       g.top[n] = top ? 1 : 0;
     }
+    });
     // next-interior node of each boundary node for the cubic-wall-energy
     // boundary phi: one step along the wall normal rounded half to even,
     // clamped to the grid (not periodic); kept only where that node is fluid
     // (fe_wetting.py:313-367)
     g.nsw.assign(N, -1);
-    for (int64_t ix = 0; ix < nx; ++ix)
+    parallel_for(nx, [&](int64_t x0, int64_t x1) {
+    for (int64_t ix = x0; ix < x1; ++ix)
       for (int64_t iy = 0; iy < ny; ++iy)
         for (int64_t iz = 0; iz < nz; ++iz) {
           const int64_t n = idx(ix, iy, iz, ny, nz);
@@ -259,12 +272,14 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
           const int64_t m = idx(t[0], t[1], t[2], ny, nz);
           if (!g.solid[m]) g.nsw[n] = (int32_t)m;
         }
+    });
   } else {
     g.nsw.assign(N, -1);
   }
   // node-class byte
   g.cls.assign(N, 0);
-  for (int64_t n = 0; n < N; ++n) {
+  parallel_for(N, [&](int64_t n0, int64_t n1) {
+  for (int64_t n = n0; n < n1; ++n) {
     uint8_t c = 0;
     if (g.solid[n]) c |= 1;
     if (g.boundary[n]) c |= 2;
@@ -277,6 +292,7 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
     c |= (uint8_t)(code << 4);
     g.cls[n] = c;
   }
+  });
   return 0;
 }
 
