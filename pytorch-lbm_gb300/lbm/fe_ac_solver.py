@@ -46,15 +46,15 @@ def _host_array(x, dtype):
 class WettingTables:
     """Read-only view of the wetting precompute (the attributes of the
     reference's ConningtonLeeWetting that callers read:
-    lbm/fe_wetting.py:140,147,305-306), as device tensors."""
+    lbm/fe_wetting.py:140,147,305-306), as device tensors made on first
+    access (the step kernels use the library's own copies; a solve that never
+    reads these pays no copy)."""
 
-    def __init__(self, solver, mode, tables):
-        dev = solver.device
+    def __init__(self, solver, mode, tables_fn):
+        self._dev = solver.device
+        self._tables_fn = tables_fn
+        self._arrays = {}
         self.mode = mode
-        self.is_boundary = torch.from_numpy(tables["is_boundary"]).to(dev)
-        self.wall_normal = torch.from_numpy(tables["wall_normal"]).to(dev)
-        self.wall_weight = torch.from_numpy(tables["wall_weight"]).to(dev)
-        self.near_wall_mask = torch.from_numpy(tables["near_wall"]).to(dev)
         cfg = solver.config
         self.theta_deg = cfg.theta_eq
         self.kappa = cfg.kappa
@@ -73,6 +73,27 @@ class WettingTables:
         else:
             self._phi_c_over_kappa = cfg.phi_c / cfg.kappa
             self._h = self._h_over_kappa = self._mu_wall = 0.0
+
+    def _get(self, key):
+        if key not in self._arrays:
+            self._arrays[key] = torch.from_numpy(self._tables_fn()[key]).to(self._dev)
+        return self._arrays[key]
+
+    @property
+    def is_boundary(self):
+        return self._get("is_boundary")
+
+    @property
+    def wall_normal(self):
+        return self._get("wall_normal")
+
+    @property
+    def wall_weight(self):
+        return self._get("wall_weight")
+
+    @property
+    def near_wall_mask(self):
+        return self._get("near_wall")
 
 
 class AllenCahnSolver:
@@ -136,7 +157,7 @@ class AllenCahnSolver:
         self.wetting = None
         self.bounce_back = None
         self.solid_fraction = None
-        self._has_partial = False
+        self._tables = None
         self._phi_wall_target = None
         if config.theta_eq != 90.0:
             c = math.cos(math.radians(config.theta_eq))
@@ -215,16 +236,28 @@ class AllenCahnSolver:
         self._solid_any = bool(solid.any())
         if frac is not None:
             self.solid_fraction = torch.tensor(frac, dtype=self.dtype, device=self.device)
-        tables = self._geometry_tables()
-        self._partial_mask = torch.from_numpy(tables["partial"]).to(self.device)
-        self._has_partial = bool(tables["partial"].any())
+        self._tables = None  # the host tables of this geometry, fetched on first use
         cfg = self.config
         if cfg.theta_eq != 90.0 and cfg.kappa > 0:
             mode = "linear" if cfg.theta_eq > 130.0 or cfg.theta_eq < 50.0 else "quadratic"
-            self.wetting = WettingTables(self, mode, tables)
+            self.wetting = WettingTables(self, mode, self._host_tables)
         else:
             self.wetting = None
         self._cache.clear()
+
+    def _host_tables(self):
+        if self._tables is None:
+            self._tables = self._geometry_tables()
+        return self._tables
+
+    @property
+    def _partial_mask(self):
+        """Partial-solid nodes (the reference's _partial_mask, lbm/fe_ac_solver.py:210)."""
+        return torch.from_numpy(self._host_tables()["partial"]).to(self.device)
+
+    @property
+    def _has_partial(self):
+        return self._geometry_set and bool(self._host_tables()["partial"].any())
 
     def _geometry_tables(self):
         N = int(np.prod(self.shape))
