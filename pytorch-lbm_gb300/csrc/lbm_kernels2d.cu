@@ -11,9 +11,12 @@
 //   k2_mu, k2_gradmu  (Cahn-Hilliard and mu-drive modes only) mu of every
 //              node, then its isotropic gradient;
 //   k2_update  stencils, wetting, forces, velocity, both BGK collisions.
-// 2-D grids are small (the reference's 2-D runs are a few hundred nodes on a
-// side), so these kernels favour the reference's operation order over the
-// restructured moment and collision algebra of the 3-D kernels.
+// Besides: k2_init (init_fields), k2_inject (inject_droplet), k2_observe and
+// k2_populations (attribute read-out).
+// These kernels keep the reference's operation order (divisions, per-
+// population non-equilibrium stress) instead of the restructured moment and
+// collision algebra of the 3-D kernels, and are compiled without FMA
+// contraction: float32 parity on the 2-D cases needed both.
 #include <cuda_runtime.h>
 
 #include "lbm_common.cuh"
