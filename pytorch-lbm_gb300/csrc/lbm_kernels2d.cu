@@ -345,13 +345,14 @@ __global__ void __launch_bounds__(kBlock) k2_init(Consts<T> k, State<T, T> s, co
 
 // phi of every node of this step, its grid sum and the mass-correction factor
 // (lbm/fe_ac_solver.py:385-389, 582-589).
+// Persistent: a grid of about one wave strides over the nodes, so that few
+// blocks publish partial sums.
 template <typename T, bool RAW>
 __global__ void __launch_bounds__(kBlock) k2_phi(Consts<T> k, State<T, T> s) {
-  const int n = blockIdx.x * kBlock + threadIdx.x;
   double pd = 0.0;
   unsigned long long pu = 0ull;
   bool nan = false;
-  if (n < k.N) {
+  for (int n = blockIdx.x * kBlock + threadIdx.x; n < k.N; n += gridDim.x * kBlock) {
     const uint8_t c = s.cls[n];
     T phi = T(0);
     if (!(c & kSolid)) {
@@ -736,6 +737,19 @@ __global__ void __launch_bounds__(kBlock) k2_inject(Consts<T> k, State<T, T> s, 
 
 inline int blocks_of(int N) { return (N + kBlock - 1) / kBlock; }
 
+// Blocks of the persistent phi kernel: at most one wave of the device (8
+// resident 256-thread blocks per SM at its 32 registers).
+inline int phi_blocks_of(int N) {
+  static const int wave = [] {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 1;
+    return 8 * (sms > 0 ? sms : 1);
+  }();
+  const int b = blocks_of(N);
+  return b < wave ? b : wave;
+}
+
 }  // namespace d2
 
 // ---------------------------------------------------------------------------
@@ -752,9 +766,9 @@ cudaError_t launch_init2d(const Consts<T>& k, const State<T, T>& s, const Src* p
 template <typename T>
 cudaError_t launch_step2d(const Consts<T>& k, const State<T, T>& s, bool raw, bool first, double ac, cudaStream_t st,
                           cudaEvent_t mid) {
-  const int nb = d2::blocks_of(k.N);
-  if (raw) d2::k2_phi<T, true><<<nb, kBlock, 0, st>>>(k, s);
-  else d2::k2_phi<T, false><<<nb, kBlock, 0, st>>>(k, s);
+  const int nb = d2::blocks_of(k.N), np = d2::phi_blocks_of(k.N);
+  if (raw) d2::k2_phi<T, true><<<np, kBlock, 0, st>>>(k, s);
+  else d2::k2_phi<T, false><<<np, kBlock, 0, st>>>(k, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (mid) {
