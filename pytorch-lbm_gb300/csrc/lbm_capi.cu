@@ -2,6 +2,7 @@
 // reference interface each entry point replaces: include/lbm_gb300.h).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -70,6 +71,13 @@ void fill_case_desc(void*, const Consts<T>&, const State<T, S>&, int, int, int, 
 using namespace lbm;
 
 static thread_local std::string g_err;
+
+// NVTX range around an entry point, shown by Nsight Systems / ncu --nvtx
+// (header-only NVTX: free when no tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 static int fail(int code, const std::string& msg) {
   g_err = msg;
@@ -651,6 +659,7 @@ int lbm_destroy(LbmHandle* h) {
 }
 
 int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, int fraction_dtype) {
+  NvtxRange range("lbm_set_geometry");
   if (!h || !solid) return fail(LBM_E_ARG, "lbm_set_geometry: null argument");
   if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
     return fail(LBM_E_ARG, "lbm_set_geometry: fraction and fraction_dtype disagree");
@@ -725,6 +734,7 @@ int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype) {
 }
 
 int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype, int on_device, void* stream) {
+  NvtxRange range("lbm_init_fields");
   if (!h || !phi) return fail(LBM_E_ARG, "lbm_init_fields: null argument");
   if (!h->geometry_set) return fail(LBM_E_STATE, "lbm_init_fields: call lbm_set_geometry first");
   if (src_dtype != LBM_DT_F32 && src_dtype != LBM_DT_F64) return fail(LBM_E_ARG, "lbm_init_fields: bad src_dtype");
@@ -772,6 +782,7 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
 }
 
 int lbm_step(LbmHandle* h, int nsteps, void* stream) {
+  NvtxRange range("lbm_step");
   if (!h) return fail(LBM_E_ARG, "lbm_step: null handle");
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_step: call lbm_init_fields first");
   if (nsteps < 0) return fail(LBM_E_ARG, "lbm_step: negative step count");
@@ -1085,6 +1096,7 @@ int lbm_get_scalars(LbmHandle* h, double* phi_mass_init, double* last_sum_phi, d
 }
 
 int lbm_measure(LbmHandle* h, double* out9, void* stream) {
+  NvtxRange range("lbm_measure");
   if (!h || !out9) return fail(LBM_E_ARG, "lbm_measure: null argument");
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_measure: not initialised");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -1234,6 +1246,7 @@ int lbm_load_state(LbmHandle* h, const void* host, int64_t bytes, void* stream) 
 }
 
 int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, float* cmax, void* stream) {
+  NvtxRange range("lbm_reduce");
   if (!h) return fail(LBM_E_ARG, "lbm_reduce: null handle");
   if (!h->initialized) return fail(LBM_E_STATE, "lbm_reduce: not initialised");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -1501,6 +1514,7 @@ int lbm_batch_destroy(LbmBatch* b) {
 }
 
 int lbm_batch_step(LbmBatch* b, int nsteps, void* stream) {
+  NvtxRange range("lbm_batch_step");
   if (!b) return fail(LBM_E_ARG, "lbm_batch_step: null batch");
   if (nsteps < 0) return fail(LBM_E_ARG, "lbm_batch_step: nsteps must be >= 0");
   cudaStream_t st = static_cast<cudaStream_t>(stream);

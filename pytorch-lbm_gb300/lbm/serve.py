@@ -17,8 +17,13 @@ p50 / p99 time to completion and aggregate MLUPS (node updates of all
 requests / wall time).  ``serve_sequential`` runs the same request stream
 through the plain one-case-at-a-time path for comparison.
 
+A request that fails (larger than the budget, a set-up that raises, a
+non-finite phi, cancelled, past its deadline) retires alone with
+``Result.error`` set; the others continue.
+
 The scheduling logic talks to the GPU through a backend (``GpuBackend``);
-tests substitute a simulated one.  The reference has no serving loop.
+tests substitute a simulated one and inject the failures on the host.  The
+reference has no serving loop.
 """
 from __future__ import annotations
 
@@ -33,6 +38,7 @@ class Request:
     rid: int
     case: object          # ImpactCase (grid, steps, ...)
     arrival: float        # seconds after the start of serving
+    deadline: float = None  # seconds after arrival by which it must finish (None: none)
 
 
 @dataclass
@@ -41,10 +47,11 @@ class Result:
     arrival: float
     admitted: float
     finished: float
-    steps: int
+    steps: int            # steps taken (the request's count unless it failed)
     nodes: int
     measure: dict = field(default_factory=dict)
     phi: object = None    # final phi on the host, if kept
+    error: str = None     # why the request was retired without a result (None: served)
 
     @property
     def latency(self):
@@ -88,16 +95,26 @@ class GpuBackend:
         solver.close()
         return m, phi
 
+    def healthy(self, solver):
+        """False once the case's status word reports a non-finite sum of phi
+        (lbm_status: a small synchronous copy, after the tick's steps)."""
+        from . import _native as nat
+        return not (solver.status() & nat.STATUS_NAN)
+
+    def discard(self, solver):
+        solver.close()
+
     def sync(self):
         self.torch.cuda.synchronize()
 
 
 def _stats(results, wall):
-    lat = np.array([r.latency for r in results]) if results else np.zeros(1)
+    ok = [r for r in results if r.error is None]
+    lat = np.array([r.latency for r in ok]) if ok else np.zeros(1)
     updates = float(sum(r.nodes * r.steps for r in results))
-    return {"requests": len(results), "wall_s": wall, "p50_s": float(np.percentile(lat, 50)),
-            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
-            "mlups": updates / wall / 1e6 if wall > 0 else 0.0}
+    return {"requests": len(results), "errors": len(results) - len(ok), "wall_s": wall,
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "mlups": updates / wall / 1e6 if wall > 0 else 0.0}
 
 
 def _select(active, saturate_nodes):
@@ -120,7 +137,7 @@ def _select(active, saturate_nodes):
 
 
 def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0, saturate_nodes=None,
-          clock=time.perf_counter, sleep=time.sleep):
+          cancelled=None, clock=time.perf_counter, sleep=time.sleep):
     """Continuous batching of `requests` under an HBM budget and at most
     `max_slots` resident cases (None: no limit).  With builders > 0, admitted
     cases are set up (inputs, geometry, init) by that many host threads while
@@ -128,13 +145,18 @@ def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0,
     the budget from the start of the set-up.  saturate_nodes (None: every
     resident case advances in every tick) selects shortest-remaining-work-first
     ticks that step only the resident cases closest to completion, at least
-    that many nodes of them (see _select).  Returns (results in completion
-    order, stats)."""
+    that many nodes of them (see _select).
+
+    A failing request retires with ``Result.error`` set and its memory freed,
+    without disturbing the others: a request larger than the whole budget (at
+    its arrival), a set-up that raises (``build failed: ...``), a case whose
+    status word reports a non-finite phi after a tick (``non-finite phi``), a
+    request for which ``cancelled(rid)`` turns true (``cancelled``) and one
+    still unfinished past its ``deadline`` (``deadline exceeded``); the last
+    three are checked between ticks.  Returns (results in completion order,
+    stats)."""
     from concurrent.futures import ThreadPoolExecutor
     pending = sorted(requests, key=lambda r: r.arrival)
-    for r in pending:
-        if backend.footprint(r.case) > budget_bytes:
-            raise ValueError(f"request {r.rid} needs more than the whole budget")
     pool = ThreadPoolExecutor(max_workers=builders) if builders > 0 else None
     building = {}      # rid -> (future, request, bytes)
     active = {}        # rid -> [request, solver, remaining steps, bytes, admitted]
@@ -143,9 +165,20 @@ def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0,
     members = ()
     results = []
     t0 = clock()
+
+    def fail(r, adm, steps, why):
+        results.append(Result(r.rid, r.arrival, adm, clock() - t0, steps, r.case.nodes, error=why))
+
+    def overdue(r, now):
+        return (r.deadline is not None and now > r.arrival + r.deadline) or (cancelled is not None and cancelled(r.rid))
+
     try:
         while pending or active or building:
             now = clock() - t0
+            # requests that can never fit are refused on arrival
+            while pending and pending[0].arrival <= now and backend.footprint(pending[0].case) > budget_bytes:
+                r = pending.pop(0)
+                fail(r, now, 0, "exceeds the HBM budget")
             # admit, in arrival order, what has arrived and fits
             while (pending and pending[0].arrival <= now
                    and used + backend.footprint(pending[0].case) <= budget_bytes
@@ -154,16 +187,37 @@ def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0,
                 b = backend.footprint(r.case)
                 used += b
                 if pool is None:
-                    active[r.rid] = [r, backend.build(r.case), int(r.case.steps), b, clock() - t0]
+                    try:
+                        active[r.rid] = [r, backend.build(r.case), int(r.case.steps), b, clock() - t0]
+                    except Exception as e:  # a bad request fails alone
+                        used -= b
+                        fail(r, clock() - t0, 0, f"build failed: {e}")
                 else:
                     building[r.rid] = (pool.submit(backend.build, r.case), r, b)
             for rid in [k for k, v in building.items() if v[0].done()]:
                 fut, r, b = building.pop(rid)
-                active[rid] = [r, fut.result(), int(r.case.steps), b, clock() - t0]
+                try:
+                    active[rid] = [r, fut.result(), int(r.case.steps), b, clock() - t0]
+                except Exception as e:
+                    used -= b
+                    fail(r, clock() - t0, 0, f"build failed: {e}")
+            # cancelled or overdue requests leave between ticks
+            now = clock() - t0
+            gone = [k for k, a in active.items() if overdue(a[0], now)]
+            if gone:
+                if batch is not None:
+                    batch.close()
+                    batch, members = None, ()
+                for k in gone:
+                    r, solver, rem, b, adm = active.pop(k)
+                    backend.discard(solver)
+                    used -= b
+                    fail(r, adm, int(r.case.steps) - rem, "cancelled" if cancelled is not None and cancelled(r.rid)
+                         else "deadline exceeded")
             if not active:
                 if building:
                     sleep(0.002)  # a set-up is in progress
-                else:
+                elif pending:
                     sleep(max(0.0, pending[0].arrival - (clock() - t0)))  # idle until the next arrival
                 continue
             key = _select(active, saturate_nodes)
@@ -174,12 +228,22 @@ def serve(requests, backend, budget_bytes, tick=100, max_slots=None, builders=0,
                 members = key
             n = min(tick, min(active[k][2] for k in key))
             batch.run(n)
-            done = []
+            done, bad = [], []
             for k in key:
                 a = active[k]
                 a[2] -= n
-                if a[2] == 0:
+                if not backend.healthy(a[1]):
+                    bad.append(k)
+                elif a[2] == 0:
                     done.append(k)
+            if bad:
+                batch.close()
+                batch, members = None, ()
+                for k in bad:
+                    r, solver, rem, b, adm = active.pop(k)
+                    backend.discard(solver)
+                    used -= b
+                    fail(r, adm, int(r.case.steps) - rem, "non-finite phi")
             if done:
                 # retire: measuring waits for the batch's steps to finish
                 batch.close()

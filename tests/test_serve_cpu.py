@@ -35,22 +35,28 @@ class Solver:
         self.case = case
         self.steps = 0
         self.open = True
+        self.nan_at = None  # injected fault: the status word reports NaN from this step on
 
 
 class FakeBackend:
     """Per step, a batch costs (sum of its nodes) / rate seconds of simulated time."""
 
-    def __init__(self, clock, rate=1e9, bytes_per_node=200):
+    def __init__(self, clock, rate=1e9, bytes_per_node=200, fail_build=(), nan_at=None):
         self.clock, self.rate, self.bpn = clock, rate, bytes_per_node
         self.resident = []
         self.peak_bytes = 0
         self.ticks = []
+        self.fail_build = set(fail_build)  # cases (by step count) whose set-up raises
+        self.nan_at = dict(nan_at or {})    # step count -> step at which NaN appears
 
     def footprint(self, case):
         return case.nodes * self.bpn
 
     def build(self, case):
+        if case.steps in self.fail_build:
+            raise RuntimeError("injected set-up failure")
         s = Solver(case)
+        s.nan_at = self.nan_at.get(case.steps)
         self.resident.append(s)
         self.peak_bytes = max(self.peak_bytes, sum(self.footprint(x.case) for x in self.resident if x.open))
         return s
@@ -79,6 +85,12 @@ class FakeBackend:
     def finish(self, solver):
         solver.open = False
         return {"steps": solver.steps}, None
+
+    def healthy(self, solver):
+        return solver.nan_at is None or solver.steps < solver.nan_at
+
+    def discard(self, solver):
+        solver.open = False
 
     def sync(self):
         pass
@@ -121,11 +133,19 @@ def test_tight_budget_admits_in_arrival_order():
         assert a.admitted <= b.admitted
 
 
-def test_oversized_request_is_rejected():
+def test_oversized_request_is_rejected_alone():
+    """A request larger than the whole budget retires with an error on arrival;
+    the others are served."""
     clk = Clock()
     be = FakeBackend(clk)
-    with pytest.raises(ValueError):
-        serve([Request(0, Case((128, 128, 128), 10), 0.0)], be, 1000, clock=clk, sleep=clk.sleep)
+    reqs = [Request(0, Case((64, 64, 48), 100), 0.0), Request(1, Case((512, 512, 512), 10), 0.1),
+            Request(2, Case((64, 64, 48), 120), 0.2)]
+    res, st = serve(reqs, be, 64 * 64 * 48 * be.bpn * 2, tick=32, clock=clk, sleep=clk.sleep)
+    by = {r.rid: r for r in res}
+    assert by[1].error == "exceeds the HBM budget" and by[1].steps == 0
+    assert by[0].error is None and by[2].error is None
+    assert by[0].measure["steps"] == 100 and by[2].measure["steps"] == 120
+    assert st["errors"] == 1
 
 
 def test_batching_never_takes_longer_than_sequential():
@@ -192,3 +212,57 @@ def test_select_order():
     assert _select(active, 15) == (1, 3)
     assert _select(active, 1015) == (1, 2, 3)
     assert _select(active, 10 ** 9) == (0, 1, 2, 3)
+
+
+
+@pytest.mark.parametrize("builders", [0, 2])
+def test_failed_setup_retires_alone(builders):
+    """A set-up that raises retires that request with an error and frees its
+    budget; every other request is served exactly."""
+    reqs = _requests()
+    bad = reqs[4].case.steps  # cases with this step count fail to build
+    clk = Clock()
+    be = FakeBackend(clk, fail_build=[bad])
+    res, st = serve(reqs, be, 10 ** 12, tick=64, builders=builders, clock=clk, sleep=clk.sleep)
+    assert sorted(r.rid for r in res) == [r.rid for r in reqs]
+    for r in res:
+        req = reqs[r.rid]
+        if req.case.steps == bad:
+            assert r.error.startswith("build failed") and r.steps == 0
+        else:
+            assert r.error is None and r.measure["steps"] == req.case.steps
+    assert st["errors"] == sum(1 for r in reqs if r.case.steps == bad)
+
+
+def test_non_finite_case_retires_alone():
+    """A case whose status word reports NaN after a tick leaves the batch with
+    an error; the cases it shared ticks with continue and finish exactly."""
+    reqs = _requests()
+    bad = reqs[1].case.steps
+    clk = Clock()
+    be = FakeBackend(clk, nan_at={bad: 100})
+    res, st = serve(reqs, be, 10 ** 12, tick=64, clock=clk, sleep=clk.sleep)
+    for r in res:
+        req = reqs[r.rid]
+        if req.case.steps == bad:
+            assert r.error == "non-finite phi" and 100 <= r.steps < req.case.steps
+        else:
+            assert r.error is None and r.measure["steps"] == req.case.steps
+    assert st["errors"] >= 1
+
+
+def test_cancel_and_deadline():
+    """A request that is cancelled, or still running past its deadline, leaves
+    between ticks with an error; the others are served exactly."""
+    reqs = _requests()
+    reqs[2] = Request(reqs[2].rid, reqs[2].case, reqs[2].arrival, deadline=0.001)
+    clk = Clock()
+    be = FakeBackend(clk)
+    res, st = serve(reqs, be, 10 ** 12, tick=16, cancelled=lambda rid: rid == 5, clock=clk, sleep=clk.sleep)
+    by = {r.rid: r for r in res}
+    assert by[5].error == "cancelled" and by[5].steps < reqs[5].case.steps
+    assert by[2].error == "deadline exceeded" and by[2].steps < reqs[2].case.steps
+    for rid, r in by.items():
+        if rid not in (2, 5):
+            assert r.error is None and r.measure["steps"] == reqs[rid].case.steps
+    assert st["errors"] == 2
