@@ -681,15 +681,21 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
       CUDA_TRY(cudaMemcpy(h->cubic, c4, sizeof(c4), cudaMemcpyHostToDevice));
     }
   }
-  if (h->prec != LBM_F64) {
-    std::vector<float> eps(N, 0.0f);
-    if (!h->geo.fraction.empty())
-      for (int64_t n = 0; n < N; ++n) eps[n] = (float)h->geo.fraction[n];
-    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * sizeof(float), cudaMemcpyHostToDevice));
+  // the penalisation fraction in the compute type: the caller's array itself
+  // when its type matches, else converted; zero without a fraction
+  const size_t ts = h->prec == LBM_F64 ? sizeof(double) : sizeof(float);
+  if (fraction_dtype == 0) {
+    CUDA_TRY(cudaMemset(h->eps, 0, N * ts));
+  } else if ((fraction_dtype == 1) == (h->prec != LBM_F64)) {
+    CUDA_TRY(cudaMemcpy(h->eps, fraction, N * ts, cudaMemcpyHostToDevice));
+  } else if (h->prec != LBM_F64) {
+    std::vector<float> eps(N);
+    for (int64_t n = 0; n < N; ++n) eps[n] = (float)static_cast<const double*>(fraction)[n];
+    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * ts, cudaMemcpyHostToDevice));
   } else {
-    std::vector<double> eps(N, 0.0);
-    if (!h->geo.fraction.empty()) eps = h->geo.fraction;
-    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<double> eps(N);
+    for (int64_t n = 0; n < N; ++n) eps[n] = (double)static_cast<const float*>(fraction)[n];
+    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * ts, cudaMemcpyHostToDevice));
   }
   float lut[kWwCodes];
   near_wall_weights(lut);

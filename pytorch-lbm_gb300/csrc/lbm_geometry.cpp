@@ -51,8 +51,8 @@ void parallel_for(int64_t n, Fn fn) {
 // (-0 where -grad/|grad| is negative or -0), as in the reference's array.
 // A 2-D grid (nz == 1) has two axes; its third component is 0.
 template <typename F>
-void smooth_normals(const F* frac, const std::vector<uint8_t>& bnd, int64_t nx, int64_t ny, int64_t nz,
-                    std::vector<float>& wn) {
+void smooth_normals(const F* frac, const HostVec<uint8_t>& bnd, int64_t nx, int64_t ny, int64_t nz,
+                    HostVec<float>& wn) {
   const int64_t N = nx * ny * nz;
   const bool two_d = nz == 1;
   auto grad_axis = [&](int64_t ix, int64_t iy, int64_t iz, int axis) -> F {
@@ -98,34 +98,32 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
   const bool two_d = nz == 1;
   const int nq = two_d ? kQ2 : kQ;
   const int(*E)[3] = two_d ? kE2 : kE;
-  g.solid.assign(N, 0);
-  g.partial.assign(N, 0);
-  g.fraction.assign(0, 0.0);
-  if (fraction_dtype != 0) g.fraction.resize(N);
+  for (auto* v : {&g.solid, &g.partial, &g.boundary, &g.near_wall, &g.top, &g.cls, &g.dist}) v->resize(N);
+  g.wall_normal.resize(3 * N);
+  g.wall_weight.resize(N);
+  g.nsw.resize(N);
+  g.has_fraction = fraction_dtype != 0;
+  g.n_boundary = 0;
+  // every table's initial value, in parallel (this also touches the pages first)
   parallel_for(N, [&](int64_t n0, int64_t n1) {
     for (int64_t n = n0; n < n1; ++n) {
       g.solid[n] = solid_in[n] ? 1 : 0;
-      if (fraction_dtype == 0) continue;
-      bool part;
+      bool part = false;
       if (fraction_dtype == 1) {
         const float v = static_cast<const float*>(fraction)[n];
-        g.fraction[n] = (double)v;
         part = v > 0.01f && v < 0.99f;
-      } else {
+      } else if (fraction_dtype == 2) {
         const double v = static_cast<const double*>(fraction)[n];
-        g.fraction[n] = v;
         part = v > 0.01 && v < 0.99;
       }
       g.partial[n] = (part && !g.solid[n]) ? 1 : 0;
+      g.boundary[n] = g.near_wall[n] = g.top[n] = 0;
+      g.dist[n] = 100;
+      g.wall_weight[n] = 0.0f;
+      g.nsw[n] = -1;
+      g.wall_normal[n] = g.wall_normal[N + n] = g.wall_normal[2 * N + n] = 0.0f;
     }
   });
-  g.boundary.assign(N, 0);
-  g.near_wall.assign(N, 0);
-  g.top.assign(N, 0);
-  g.wall_normal.assign(3 * N, 0.0f);
-  g.wall_weight.assign(N, 0.0f);
-  g.dist.assign(N, 100);
-  g.n_boundary = 0;
 
   if (wetting) {
     // boundary: fluid node whose periodic neighbour x - e_q is solid for some
@@ -200,7 +198,7 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
                                idx(ix, iy, wrap(iz - 1, nz), ny, nz), idx(ix, iy, wrap(iz + 1, nz), ny, nz)};
         for (int64_t m : nb)
           if (g.dist[m] == 100) {
-            g.dist[m] = pass;
+            g.dist[m] = (uint8_t)pass;
             next.push_back(m);
           }
       }
@@ -256,7 +254,6 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
     // boundary phi: one step along the wall normal rounded half to even,
     // clamped to the grid (not periodic); kept only where that node is fluid
     // (fe_wetting.py:313-367)
-    g.nsw.assign(N, -1);
     parallel_for(nx, [&](int64_t x0, int64_t x1) {
     for (int64_t ix = x0; ix < x1; ++ix)
       for (int64_t iy = 0; iy < ny; ++iy)
@@ -273,11 +270,8 @@ int compute_geometry(int64_t nx, int64_t ny, int64_t nz, const uint8_t* solid_in
           if (!g.solid[m]) g.nsw[n] = (int32_t)m;
         }
     });
-  } else {
-    g.nsw.assign(N, -1);
   }
   // node-class byte
-  g.cls.assign(N, 0);
   parallel_for(N, [&](int64_t n0, int64_t n1) {
   for (int64_t n = n0; n < n1; ++n) {
     uint8_t c = 0;
