@@ -261,7 +261,10 @@ int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, f
  * solid: device, nx*ny*nz bytes, 1 = solid, 0 = fluid (a torch.bool tensor);
  * out9: device, 9 doubles, written as by lbm_measure (volume, C_max, Dx, Dy,
  * Dz, k, z centre, count, NaN flag).  Asynchronous on `stream`.  Grids of more
- * than LBM_MEASURE_STATIC_MAX_NODES nodes are rejected with LBM_E_ARG.
+ * than LBM_MEASURE_STATIC_MAX_NODES nodes are rejected with LBM_E_ARG.  A 2-D
+ * (nx, ny) field passed as the grid 1 x nx x ny gets its x and y extents in
+ * out9[3] and out9[4] and its centre along y in out9[6] (the reference's
+ * 2-D Dx, Dy; its Dz is 0).
  *
  * The first call on a device looks up the static array's device address
  * (this may load the library's kernels onto that device), so make it before

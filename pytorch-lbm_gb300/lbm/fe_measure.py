@@ -1,7 +1,7 @@
 """Droplet measurements with the reference's functions and return values
 (pytorch-lbm ``lbm/fe_measure.py``): spread factors and the wall contact angle.
 
-``measure_spread_factor`` reduces a CUDA field on the device (the library's
+``measure_spread_factor`` reduces a 2-D or 3-D CUDA field on the device (the library's
 allocation-free spread reduction, ``lbm_measure_static``), so a caller that
 polls a running solve copies 9 numbers to the host instead of the field;
 host arrays and 2-D fields are measured on the host.  ``measure_contact_angle``
@@ -32,7 +32,10 @@ def _empty(volume, c_max):
 
 def _spread_device(C, solid_mask):
     from . import _native as nat
-    nx, ny, nz = C.shape
+    two_d = C.dim() == 2
+    # a 2-D field is reduced as the 1 x nx x ny grid of the same memory layout:
+    # its "y" and "z" extents are then Dx and Dy
+    nx, ny, nz = (1,) + tuple(C.shape) if two_d else tuple(C.shape)
     phi = C.detach().contiguous()
     if phi.dtype not in (torch.float32, torch.float64):
         phi = phi.to(torch.float32)
@@ -49,7 +52,7 @@ def _spread_device(C, solid_mask):
     volume, c_max, count = float(v[0]), float(v[1]), int(v[7])
     if count == 0:
         return _empty(volume, c_max)
-    Dx, Dy, Dz = float(v[2]), float(v[3]), float(v[4])
+    Dx, Dy, Dz = (float(v[3]), float(v[4]), 0.0) if two_d else (float(v[2]), float(v[3]), float(v[4]))
     return {"Dx": Dx, "Dy": Dy, "Dz": Dz, "k": Dx / Dy if Dy > 0 else 0.0, "volume": volume, "C_max": c_max}
 
 
@@ -57,9 +60,9 @@ def measure_spread_factor(C, solid_mask=None) -> dict:
     """Extents Dx, Dy, Dz of the C > 0.5 set (solid nodes excluded), k = Dx / Dy,
     volume = sum of C with solid nodes zeroed, C_max (lbm/fe_measure.py:11-82).
 
-    A 3-D CUDA tensor is reduced on its device (the volume summed in float64);
-    anything else on the host."""
-    if torch is not None and isinstance(C, torch.Tensor) and C.is_cuda and C.dim() == 3:
+    A 2-D or 3-D CUDA tensor is reduced on its device (the volume summed in
+    float64); anything else on the host."""
+    if torch is not None and isinstance(C, torch.Tensor) and C.is_cuda and C.dim() in (2, 3):
         return _spread_device(C, solid_mask)
     c = np.array(_host(C), copy=True)
     if solid_mask is not None:

@@ -45,7 +45,7 @@ def test_empty_interface():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", [n for n in sorted(inputs()) if inputs()[n][0].ndim == 3])
+@pytest.mark.parametrize("name", sorted(inputs()))
 def test_device_spread_equals_reference(name, ref, built_lib):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
