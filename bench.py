@@ -11,8 +11,10 @@ reference's generators).
 One "step" is one lattice time step of the whole grid.  Reported:
   value      MLUPS (million lattice-node updates per second) over K timed
              steps (one lbm_step call) with the state resident on the device,
-             CUDA events on the launching stream.  The state (f, g: 732 MB)
-             is larger than L2, so no flush is needed between steps.
+             CUDA events on the launching stream.  The K-step region is
+             repeated until --min-seconds of device time have passed and the
+             median repetition is reported.  The state (f, g: 732 MB) is
+             larger than L2, so no flush is needed between steps.
   e2e        the same metric through the public API (AllenCahnSolver) from
              host numpy arrays: construction, set_solid, init_fields (H2D),
              K steps, the sweep drivers' read of phi to host every 50 steps
@@ -22,7 +24,10 @@ One "step" is one lattice time step of the whole grid.  Reported:
              the kernels), against the measured HBM copy peak; step_roofline:
              the whole step's 336 B/node over the timed region.
   cpu_baseline  the numpy oracle (oracle/ac_oracle.py) on a bounded sample of
-             the same workload, one host core.
+             the same workload, one host core; the reference's own PyTorch
+             CPU figure, measured where the reference is installed, beside it.
+  fp64_error the e2e run's phi, u, sum(phi) drift and spread factor after K
+             steps against a float64 run of the same configuration.
 
 --impl reference times the CPU implementation of the path (the oracle port;
 the reference itself is Python/PyTorch and is not present on the GPU host)
@@ -283,18 +288,29 @@ def run_ours(args, rank, world, device):
         s.step()
     lib, h = s._lib, s._h
     stream = torch.cuda.current_stream(device)
-    # timed region: K steps in one lbm_step call, CUDA events on the launching stream
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier(world)
-    torch.cuda.synchronize(device)
+    # timed region: K steps in one lbm_step call, CUDA events on the launching
+    # stream, bracketed by a barrier and a device synchronisation.  The K-step
+    # region is repeated until at least --min-seconds of device time have
+    # passed (so that the clock sampler sees the load) and the median
+    # repetition is reported.
+    reps_ms = []
     with Clocks(device.index) as clk:
-        e0.record(stream)
-        nat.check(lib.lbm_step(h, K, nat.stream_ptr(stream)), "lbm_step")
-        e1.record(stream)
-        torch.cuda.synchronize(device)
-    barrier(world)
-    s.step_count += K
-    tot_ms = e0.elapsed_time(e1)
+        while True:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            barrier(world)
+            torch.cuda.synchronize(device)
+            e0.record(stream)
+            nat.check(lib.lbm_step(h, K, nat.stream_ptr(stream)), "lbm_step")
+            e1.record(stream)
+            torch.cuda.synchronize(device)
+            barrier(world)
+            s.step_count += K
+            reps_ms.append(e0.elapsed_time(e1))
+            # every rank repeats as often as rank 0 decides
+            more = sum(reps_ms) < args.min_seconds * 1e3 and len(reps_ms) < args.max_reps
+            if not bcast_flag(more, world, device):
+                break
+    tot_ms = statistics.median(reps_ms)
     # per-kernel durations: a separate pass with events recorded between the
     # two kernels of every step (which serialises them: durations are upper bounds)
     Kp = min(K, 200)
@@ -327,6 +343,8 @@ def run_ours(args, rank, world, device):
     torch.cuda.synchronize(device)
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world, device)
+    s2_fields = [x.double().cpu().numpy() for x in s2.fields("phi", "u")]
+    s2_meas = dict(m2, phi_mass_init=s2.phi_mass_init)
     s2.close()
     # the same run with the sweep drivers' every-50-steps check (extents, z
     # centre, NaN) reduced on the device instead of copying phi to the host
@@ -346,6 +364,11 @@ def run_ours(args, rank, world, device):
     e2e = replica_mlups(n, K, e2e_s * 1e3, world)
     h2d = solid.nbytes + frac.nbytes + C.nbytes + u.nbytes
     d2h = reads * n * 4 + 9 * 8
+    # the error of this run (K steps from the initial state, the e2e solve)
+    # against a float64 run of the same configuration and inputs
+    fp64 = None
+    if rank == 0 and not args.no_fp64_check:
+        fp64 = fp64_error(s2_fields, s2_meas, cfg, solid, frac, C, u, skw, K, WORKLOADS[name]["radius"])
 
     out = None
     if rank == 0:
@@ -373,10 +396,18 @@ def run_ours(args, rank, world, device):
             cm, cdt = cpu_oracle_mlups(name, args.cpu_steps, warmup=1)
             cpu = {"value": cm, "unit": "MLUPS", "cores": 1, "kind": "port",
                    "sample": f"{args.cpu_steps} steps (+1 warm-up) of the full grid, numpy oracle, "
-                             f"{cdt:.1f} s"}
+                             f"{cdt:.1f} s",
+                   "what": "one host core running the numpy restatement of the reference step (numpy "
+                           "array operations are single-threaded); the reference itself is PyTorch and "
+                           "does not exist on this host",
+                   "reference_torch_cpu": REF_TORCH_CPU.get(name)}
         out = {
             "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": tot_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": tot_ms / K,
+            "timed_reps": {"reps": len(reps_ms), "ms_per_rep_median": tot_ms, "ms_per_rep_min": min(reps_ms),
+                           "ms_per_rep_max": max(reps_ms), "device_s_total": sum(reps_ms) / 1e3,
+                           "what": f"the K-step region repeated until >= {args.min_seconds} s of device time; "
+                                   "value and ms_per_step from the median repetition"}, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["label"], "nodes": n,
                        "precision": ("fp16 deviation-stored populations, fp32 math and fields, fp64 global sum"
@@ -408,6 +439,7 @@ def run_ours(args, rank, world, device):
             # two kernels per step (four with the mu and grad-mu passes of the grad-mu modes)
             "gpu_launches": ((4 if args.mode in ("cahn-hilliard", "mu-drive") else 2) * K) if two_kernel else K,
             "cpu_baseline": cpu,
+            "fp64_error": fp64,
             "clocks": clk.summary(),
             "spread_after": {k2: meas[k2] for k2 in ("Dx", "Dy", "k", "z_com", "volume")},
         }
@@ -575,6 +607,58 @@ def run_serve(args, device):
             "srpt_p99_ratio": st_r["p99_s"] / st_s["p99_s"]}
 
 
+# The reference's own PyTorch CPU path on the drop-in cases, measured where the
+# reference is installed (8-core Xeon @ 2.7 GHz, torch 2.11 CPU build, 8
+# intra-op threads): it does not exist on the GPU host, so it is reported
+# beside the numpy port that is timed there.
+REF_TORCH_CPU = {
+    "ridge150": {"mlups": 1.98, "ms_per_step": 1213.7, "cores": 8, "dtype": "float32",
+                 "where": "8-core Xeon @ 2.7 GHz, torch 2.11 CPU, 5 steps"},
+    "flat64": {"mlups": 3.04, "ms_per_step": 64.7, "cores": 8, "dtype": "float32",
+               "where": "8-core Xeon @ 2.7 GHz, torch 2.11 CPU, 20 steps"},
+}
+
+
+def fp64_error(fields, meas, cfg, solid, frac, C, u, skw, K, radius):
+    """Error of a run's phi, u, sum(phi) drift and spread factor after K steps
+    against a float64 run of the same configuration from the same inputs."""
+    import torch
+    from lbm.fe_ac_solver import AllenCahnSolver
+    s = AllenCahnSolver(cfg, dtype=torch.float64, **skw)
+    s.set_solid(solid, frac)
+    s.init_fields(C, u)
+    s.run(K)
+    phi64, u64 = [x.cpu().numpy() for x in s.fields("phi", "u")]
+    m64 = dict(s.measure(), phi_mass_init=s.phi_mass_init)
+    s.close()
+    phi, vel = fields
+    drift = lambda m: (m["volume"] - m["phi_mass_init"]) / m["phi_mass_init"]
+    beta = lambda m: max(m["Dx"], m["Dy"]) / (2.0 * radius)
+    return {"steps": K,
+            "max_abs_dphi": float(np.abs(phi - phi64).max()),
+            "rel_l2_du": float(np.linalg.norm(vel - u64) / max(np.linalg.norm(u64), 1e-300)),
+            "sum_phi_drift": drift(meas), "sum_phi_drift_f64": drift(m64),
+            "sum_phi_drift_diff": drift(meas) - drift(m64),
+            "spread_factor": beta(meas), "spread_factor_f64": beta(m64),
+            "spread_factor_rel_err": abs(beta(meas) - beta(m64)) / beta(m64) if beta(m64) else None,
+            "k": meas["k"], "k_f64": m64["k"],
+            "what": "this run (the e2e solve: K steps from the initial state) against a float64 run of the "
+                    "same configuration and inputs; the 150x150x107 impact amplifies rounding differences "
+                    "(one float32 ulp of the initial state gives max|dphi| ~6e-3 by step 60), so the "
+                    "pointwise figures grow with K while the spread factor and sum(phi) drift stay close"}
+
+
+def bcast_flag(flag, world, device):
+    """Rank 0's boolean on every rank."""
+    if world == 1:
+        return flag
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([1 if flag else 0], dtype=torch.int32, device=device)
+    dist.broadcast(t, 0)
+    return bool(t.item())
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -617,6 +701,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true", help="skip the float64 run of the same workload")
+    ap.add_argument("--min-seconds", type=float, default=0.5,
+                    help="repeat the timed K-step region until this much device time has passed")
+    ap.add_argument("--max-reps", type=int, default=1000)
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--mode", default="default", choices=sorted(MODES),

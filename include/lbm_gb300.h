@@ -266,12 +266,20 @@ int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, f
  * out9[3] and out9[4] and its centre along y in out9[6] (the reference's
  * 2-D Dx, Dy; its Dz is 0).
  *
- * The first call on a device looks up the static array's device address
- * (this may load the library's kernels onto that device), so make it before
- * any stream capture.  Every call shares the one array and leaves its
- * contents behind: calls that overlap on the GPU (two streams, or two host
- * threads on one device) race and must be serialised by the caller.  No
- * counterpart in the reference: an addition of this library. */
+ * The first call on a device looks up the static array's device address.
+ * Under the CUDA runtime's default lazy module loading that lookup may load
+ * the library's module onto the device, and loading places the static array
+ * in device memory: an allocation made by the driver on the first call.  A
+ * caller that may not allocate after start-up therefore makes one call per
+ * device during start-up (or runs with CUDA_MODULE_LOADING=EAGER); the same
+ * first call must come before any stream capture.  Later calls allocate
+ * nothing.  The address is cached per device ordinal and belongs to the
+ * device's primary context (the one the CUDA runtime uses); a caller that
+ * makes another context current through the driver API must not call this.
+ * Every call shares the one array and leaves its contents behind: calls
+ * that overlap on the GPU (two streams, or two host threads on one device)
+ * race and must be serialised by the caller.  No counterpart in the
+ * reference: an addition of this library. */
 int lbm_measure_static(int64_t nx, int64_t ny, int64_t nz, const void* phi, int phi_dtype,
                        const uint8_t* solid, double* out9, void* stream);
 

@@ -4,13 +4,22 @@
 ``measure_spread_factor`` reduces a 2-D or 3-D CUDA field on the device (the library's
 allocation-free spread reduction, ``lbm_measure_static``), so a caller that
 polls a running solve copies 9 numbers to the host instead of the field;
-host arrays and 2-D fields are measured on the host.  ``measure_contact_angle``
+host arrays and CPU tensors are measured on the host.  ``measure_contact_angle``
 scans one wall layer and one column, which the reference does on the host;
 it stays there.
+
+The device reduction keeps its block partials in one scratch array per GPU
+that every call shares.  This module serialises its own calls (a lock per
+device, held from the launch until the 9 results are on the host), so threads
+of one process that measure fields on different streams get correct results;
+another caller of the C entry point on the same device must not overlap with
+it.  The call synchronises with the device, so it cannot be made while a
+stream is being captured into a CUDA graph.
 """
 from __future__ import annotations
 
 import ctypes
+import threading
 
 import numpy as np
 
@@ -30,6 +39,18 @@ def _empty(volume, c_max):
     return {"Dx": 0.0, "Dy": 0.0, "Dz": 0.0, "k": 0.0, "volume": volume, "C_max": c_max}
 
 
+_DEVICE_LOCKS: dict = {}
+_LOCKS_GUARD = threading.Lock()
+
+
+def _device_lock(index):
+    with _LOCKS_GUARD:
+        lk = _DEVICE_LOCKS.get(index)
+        if lk is None:
+            lk = _DEVICE_LOCKS[index] = threading.Lock()
+        return lk
+
+
 def _spread_device(C, solid_mask):
     from . import _native as nat
     two_d = C.dim() == 2
@@ -45,11 +66,16 @@ def _spread_device(C, solid_mask):
         solid = torch.as_tensor(solid_mask, device=C.device).to(torch.bool).contiguous().view(torch.uint8)
     out = torch.empty(9, dtype=torch.float64, device=C.device)
     dt = nat.LBM_DT_F32 if phi.dtype == torch.float32 else nat.LBM_DT_F64
-    with torch.cuda.device(C.device):
+    # the reduction's scratch is shared by every call on the device: one call at a time,
+    # from the launch until its results have reached the host
+    with torch.cuda.device(C.device), _device_lock(C.device.index):
         nat.check(nat.lib().lbm_measure_static(nx, ny, nz, nat.ptr(phi), dt, ctypes.c_void_p(solid.data_ptr()),
                                                nat.ptr(out), nat.stream_ptr()), "lbm_measure_static")
         v = out.cpu().numpy()
     volume, c_max, count = float(v[0]), float(v[1]), int(v[7])
+    if v[8] != 0.0:
+        # a NaN node: numpy's max (the reference's C_max) is NaN; the device maximum skips NaN
+        c_max = float("nan")
     if count == 0:
         return _empty(volume, c_max)
     Dx, Dy, Dz = (float(v[3]), float(v[4]), 0.0) if two_d else (float(v[2]), float(v[3]), float(v[4]))
@@ -61,7 +87,14 @@ def measure_spread_factor(C, solid_mask=None) -> dict:
     volume = sum of C with solid nodes zeroed, C_max (lbm/fe_measure.py:11-82).
 
     A 2-D or 3-D CUDA tensor is reduced on its device (the volume summed in
-    float64); anything else on the host."""
+    float64); anything else on the host.  A field with a NaN node gives a NaN
+    volume and C_max, as numpy's sum and max do in the reference.
+
+    On the device the reduction uses one scratch array per GPU shared by all
+    calls (it allocates no device memory).  Calls from this module are
+    serialised per device; they synchronise with the device, so none may be
+    made during CUDA graph capture, and a caller of the C entry point
+    ``lbm_measure_static`` on the same device must not run concurrently."""
     if torch is not None and isinstance(C, torch.Tensor) and C.is_cuda and C.dim() in (2, 3):
         return _spread_device(C, solid_mask)
     c = np.array(_host(C), copy=True)

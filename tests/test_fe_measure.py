@@ -59,3 +59,70 @@ def test_device_spread_equals_reference(name, ref, built_lib):
             assert m[k] == r[k], k
         # float64 sum on the device against numpy's float32 pairwise sum
         assert m["volume"] == pytest.approx(r["volume"], rel=2e-6 if phi.dtype == np.float32 else 1e-12)
+
+
+def _nan_field():
+    phi, solid = inputs()["cap3d_zc2.0"]
+    phi = phi.copy()
+    # one NaN node in the fluid, away from the wall
+    idx = tuple(int(s) // 2 for s in phi.shape)
+    phi[idx] = np.nan
+    assert not solid[idx]
+    return phi, solid
+
+
+def test_host_nan_field_gives_nan_volume_and_cmax():
+    """numpy's sum and max propagate NaN (the reference's volume and C_max)."""
+    from lbm.fe_measure import measure_spread_factor
+    phi, solid = _nan_field()
+    m = measure_spread_factor(phi, solid)
+    assert np.isnan(m["volume"]) and np.isnan(m["C_max"])
+    assert m["Dx"] > 0
+
+
+@pytest.mark.gpu
+def test_device_nan_field_matches_host(built_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    from lbm.fe_measure import measure_spread_factor
+    phi, solid = _nan_field()
+    host = measure_spread_factor(phi, solid)
+    dev = measure_spread_factor(torch.from_numpy(phi).cuda(), torch.from_numpy(solid).cuda())
+    for k in ("Dx", "Dy", "Dz", "k"):
+        assert dev[k] == host[k], k
+    assert np.isnan(dev["volume"]) and np.isnan(dev["C_max"])
+
+
+@pytest.mark.gpu
+def test_device_measurements_from_concurrent_threads(ref, built_lib):
+    """Host threads measuring different fields on their own streams share the
+    device scratch of the reduction; the module serialises them, so every
+    result equals the reference's."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    import threading
+    from lbm.fe_measure import measure_spread_factor
+    names = [n for n in sorted(inputs()) if inputs()[n][0].ndim == 3]
+    fields = {n: (torch.from_numpy(inputs()[n][0]).cuda(), torch.from_numpy(inputs()[n][1]).cuda())
+              for n in names}
+    torch.cuda.synchronize()
+    errors = []
+
+    def work(offset):
+        stream = torch.cuda.Stream()
+        with torch.cuda.stream(stream):
+            for i in range(12):
+                n = names[(i + offset) % len(names)]
+                m = measure_spread_factor(*fields[n])
+                r = ref[n]["spread"]
+                if any(m[k] != r[k] for k in ("Dx", "Dy", "Dz", "k", "C_max")):
+                    errors.append((n, m, r))
+
+    threads = [threading.Thread(target=work, args=(j,)) for j in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:2]

@@ -2,9 +2,11 @@
 device memory (code inside another runtime's memory pool, a driver that forbids
 allocation after start-up, a monitoring hook that must not disturb the solve's
 allocator).  It keeps its reduction scratch in a static device array of the
-library, so the check here is that it gives what lbm_measure gives, on two
+library, so the checks here are that it gives what lbm_measure gives, on two
 calls in a row (the second one finds the first one's partials and counter
-left in the shared array), and that it refuses grids above its maximum.
+left in the shared array), that calls after the first leave the device's free
+memory and the torch allocator's counters unchanged, and that it refuses grids
+above its maximum.
 
 Collected last on purpose (the file name sorts after every other test file)."""
 import ctypes
@@ -66,6 +68,44 @@ def test_measure_static_matches_lbm_measure(built_lib, dn):
         ref = _handle(built_lib, s)
         _compare(got, ref)
         assert got[7] > 0 and got[8] == 0.0
+
+
+@pytest.mark.gpu
+def test_measure_static_allocates_nothing(built_lib):
+    """After the first call (which may load the module and its static array
+    onto the device), further calls change neither cudaMemGetInfo's free
+    bytes nor the torch caching allocator's counters."""
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    from lbm import _native as nat
+    from lbm.fe_ac_solver import AllenCahnSolver
+    case = CASES["ridge_l162"]
+    solid, frac, C, u = inputs(case)
+    s = AllenCahnSolver(config(case, "cuda"), dtype=torch.float32, **case["kw"])
+    s.set_solid(solid, frac)
+    s.init_fields(C, u)
+    s.run(3)
+    nx, ny, nz = s.shape
+    phi = s.phi.contiguous()
+    solid_d = s.solid.contiguous()
+    outs = [torch.full((9,), -7.0, dtype=torch.float64, device=phi.device) for _ in range(6)]
+    stream = nat.stream_ptr()
+    args = (nx, ny, nz, nat.ptr(phi), nat.LBM_DT_F32, nat.ptr(solid_d))
+    nat.check(built_lib.lbm_measure_static(*args, nat.ptr(outs[0]), stream), "lbm_measure_static")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    for out in outs[1:]:
+        nat.check(built_lib.lbm_measure_static(*args, nat.ptr(out), stream), "lbm_measure_static")
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert free1 == free0
+    for key in ("allocation.all.allocated", "segment.all.allocated", "reserved_bytes.all.current"):
+        assert stats1.get(key, 0) == stats0.get(key, 0), key
+    first = outs[0].cpu().numpy()
+    for out in outs[1:]:
+        assert np.array_equal(out.cpu().numpy(), first)
 
 
 def test_measure_static_rejects_oversized_grid(built_lib):
