@@ -271,6 +271,8 @@ def run_ours(args, rank, world, device):
     skw = solver_kwargs(args.mode, tuple(cfg.grid_shape))
     s = AllenCahnSolver(cfg, dtype=pdt, **skw)
     s.set_solid(solid, frac)
+    if args.layout != "auto":
+        s.set_layout(args.layout == "paired")
     s.init_fields(C, u)
     for _ in range(W):
         s.step()
@@ -414,6 +416,7 @@ def run_ours(args, rank, world, device):
                                      if f16 else "fp32 populations, fp32 math, fp64 global sum"),
                        "parallelism": "replicas" if world > 1 else "single",
                        "mode": args.mode,
+                       "layout": "paired" if s.paired else "linear",
                        "tile": list(tile), "tuned_ms": tune_ms,
                        "l2": f"state (f, g: {4 * s.lattice.q * n * (2 if f16 else 4) / 1e6:.0f} MB) larger "
                              "than L2 (129 MB): no flush"},
@@ -710,6 +713,8 @@ def main():
     ap.add_argument("--mode", default="default", choices=sorted(MODES),
                     help="solver option variant of the drop-in case (the bench line's config names it)")
     ap.add_argument("--tile", default=None, help="fixed tile 'tx,ty,tz' of the step kernel (no autotune)")
+    ap.add_argument("--layout", default="auto", choices=["auto", "paired", "linear"],
+                    help="state storage layout of the timed solver (auto: the library's default, linear)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -111,14 +111,21 @@ int lbm_destroy(LbmHandle* h);
 
 /* Solid mask (host, N bytes, nonzero = solid) and optional solid fraction
  * (host, N elements of fraction_dtype, or NULL with LBM_DT_NONE).  Computes
- * on the host, bit-exact with the reference: partial-solid nodes and their
+ * on the device, bit-exact with the reference: partial-solid nodes and their
  * penalisation fraction, wetting boundary nodes, wall normals (smooth from the
- * fraction gradient, else discrete), near-wall distance and weight; uploads
- * the node-class table.  Replaces AllenCahnSolver.set_solid
+ * fraction gradient, else discrete), near-wall distance and weight, the
+ * top-surface flag and the node-class table.  Replaces AllenCahnSolver.set_solid
  * (lbm/fe_ac_solver.py:193-237) and ConningtonLeeWetting.__init__ /
  * _precompute_* (lbm/fe_wetting.py:39-367).  Synchronous. */
 int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction,
                      int fraction_dtype);
+
+/* As lbm_set_geometry with the solid mask and the fraction in device memory
+ * (N bytes and N elements of fraction_dtype), asynchronous on `stream`; both
+ * must stay valid until the work queued on `stream` has run.  Replaces the
+ * same reference code as lbm_set_geometry. */
+int lbm_set_geometry_device(LbmHandle* h, const uint8_t* solid, const void* fraction,
+                            int fraction_dtype, void* stream);
 
 /* Per-node geometric amplification field alpha (host, N elements of
  * alpha_dtype, LBM_DT_F32 or LBM_DT_F64), used in place of the scalar
@@ -161,6 +168,22 @@ int lbm_step_profiled(LbmHandle* h, int nsteps, void* stream, float* kernel_ms3)
  * the two-kernel step.  No reference counterpart (a GB300 launch parameter). */
 int lbm_set_tile(LbmHandle* h, int tx, int ty, int tz);
 int lbm_get_tile(LbmHandle* h, int* txyz3);
+
+/* Storage layout of the state arrays.  paired = 0 (the default): one
+ * element per node in node order, stepped one thread per node.  paired = 1
+ * (3-D grids with an even nx in LBM_F32 or LBM_F16 only): nodes x and
+ * x + nx/2 of the same (y, z) share one 8-byte (float) or 4-byte (half) word
+ * of every population, u and phi array, and the step runs one thread per such
+ * pair with packed two-node loads, stores and f32x2 arithmetic: fewer
+ * instructions per node, but at 128 registers per thread half as many
+ * threads per SM (slower on the 150x150x107 ridge case on GB300).  Both layouts compute the same
+ * step; they may differ in the last float32 bits (the compiler contracts
+ * multiply-adds differently in the two kernels).  Call before
+ * lbm_init_fields (LBM_E_STATE afterwards); LBM_E_UNSUPPORTED for a paired
+ * request the grid or precision cannot take.  lbm_get_layout reports the
+ * handle's layout.  No reference counterpart (a GB300 memory layout). */
+int lbm_set_layout(LbmHandle* h, int paired);
+int lbm_get_layout(LbmHandle* h, int* paired);
 
 /* Step autotuner: times `reps` launches of the next step for the two-kernel
  * step and for each candidate tile shape of the fused kernel on the handle's

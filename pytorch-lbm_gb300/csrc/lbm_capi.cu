@@ -37,7 +37,7 @@ template <typename T>
 cudaError_t launch_measure(int, int, int, const T*, const uint8_t*, double*, int, unsigned*, double*,
                            cudaStream_t, double* = nullptr);
 template <typename T>
-cudaError_t launch_momentum(int, const T*, const T*, int, double, double, double*, int, unsigned*, double*,
+cudaError_t launch_momentum(int, const T*, const T*, int, int, double, double, double*, int, unsigned*, double*,
                             cudaStream_t);
 template <typename T>
 cudaError_t launch_measure_static(int, int, int, const T*, const uint8_t*, double*, cudaStream_t);
@@ -47,6 +47,10 @@ template <typename T, typename S>
 cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, cudaStream_t, bool = false);
 template <typename T, typename S>
 cudaError_t launch_mu(const Consts<T>&, const State<T, S>&, cudaStream_t);
+template <typename T, typename S>
+cudaError_t launch_phi_pair(const void*, const unsigned short*, int, cudaStream_t);
+template <typename T, typename S>
+cudaError_t launch_update_pair(const void*, const unsigned short*, int, bool, cudaStream_t, bool);
 
 // the 2-D (nz == 1, D2Q9) form (lbm_kernels2d.cu)
 template <typename T, typename Src>
@@ -61,6 +65,10 @@ cudaError_t launch_populations2d(const Consts<T>&, const State<T, T>&, bool, T*,
 template <typename T>
 cudaError_t launch_inject2d(const Consts<T>&, const State<T, T>&, bool, const InjectParams&, const T*, unsigned*,
                             cudaStream_t);
+
+template <typename T>
+cudaError_t launch_geometry(int, int, int, const uint8_t*, const void*, int, bool, bool, uint8_t*, uint8_t*, float*,
+                            int*, T*, cudaStream_t);
 
 template <typename T, typename S>
 size_t case_desc_bytes();
@@ -99,6 +107,7 @@ struct LbmHandle {
   int prec = LBM_F32;
   int64_t nx = 0, ny = 0, nz = 0, N = 0;
   int64_t Np = 0;  // component stride of f, g, u: N rounded up to kAlignNodes
+  bool paired = false;  // paired layout (Consts::nh): 3-D float / half grids with even nx
   int device = 0;
   size_t tsize = 4;  // compute type (u, phi, eps, fields)
   size_t psize = 4;  // population storage type
@@ -124,7 +133,7 @@ struct LbmHandle {
   bool wetting = false;
   Consts<float> kf{};
   Consts<double> kd{};
-  Geometry geo;
+  std::vector<uint8_t> cls_host;  // node-class table on the host (lazily fetched; empty = not fetched)
   // sequencing
   bool geometry_set = false, initialized = false;
   Tiling tiling{};
@@ -156,6 +165,8 @@ Consts<T> make_consts(const LbmHandle& h, const float* ww_lut) {
   k.nz = (int)h.nz;
   k.N = (int)h.N;
   k.Np = (int)h.Np;
+  k.nh = h.paired ? (int)(h.N / 2) : 0;
+  k.hx = h.paired ? (int)(h.nx / 2) : 0;
   k.dz = make_fastdiv((unsigned)h.nz);
   k.dy = make_fastdiv((unsigned)h.ny);
   const double cs2 = 1.0 / 3.0;
@@ -421,11 +432,30 @@ bool omega1_of(const LbmHandle* h) {
 
 // Blocks of a case in the (batched) phi kernel grid, per_thread nodes per
 // thread, and in the update kernel grid (one node per thread).
+// (Pairs of nodes in the paired layout.)
+int64_t units_of(const LbmHandle* h) { return h->paired ? h->N / 2 : h->N; }
+// per_thread counts nodes (a thread of the paired kernel takes per_thread / 2 pairs).
 int phi_blocks_of(const LbmHandle* h, int per_thread) {
-  const long long per = (long long)kBlock * per_thread;
-  return (int)std::max<long long>(1, (h->N + per - 1) / per);
+  const long long per = (long long)kBlock * (h->paired ? std::max(1, per_thread / 2) : per_thread);
+  return (int)std::max<long long>(1, (units_of(h) + per - 1) / per);
 }
-int upd_blocks_of(const LbmHandle* h) { return (int)((h->N + kBlock - 1) / kBlock); }
+int upd_blocks_of(const LbmHandle* h) {
+  const int64_t bs = h->paired ? kPairUpdBlock : kBlock;
+  return (int)((units_of(h) + bs - 1) / bs);
+}
+
+// The step kernels of a grid's layout over a case table: the paired kernels
+// or the single-node kernels.
+template <typename T, typename S>
+cudaError_t launch_phi_kernel(bool paired, const void* cases, const unsigned short* b2c, int blocks, cudaStream_t st) {
+  return paired ? launch_phi_pair<T, S>(cases, b2c, blocks, st) : launch_phi_batch<T, S>(cases, b2c, blocks, st);
+}
+template <typename T, typename S>
+cudaError_t launch_update_kernel(bool paired, const void* cases, const unsigned short* b2c, int blocks, bool omega1,
+                                 cudaStream_t st, bool gmu) {
+  return paired ? launch_update_pair<T, S>(cases, b2c, blocks, omega1, st, gmu)
+                : launch_update_batch<T, S>(cases, b2c, blocks, omega1, st, gmu);
+}
 
 // The handle's one-case descriptor table for the batched kernels: [0] the
 // state as it is now, [1] after one more step.  The descriptor holds device
@@ -465,13 +495,13 @@ int launch_next(LbmHandle* h, const Tiling& t, cudaStream_t st, cudaEvent_t mid)
     const int par = (h->cur ^ h->desc_cur0) & 1;
     const bool gmu = h->mu != nullptr;
     const unsigned char* d = static_cast<const unsigned char*>(h->desc) + par * case_desc_bytes<T, S>();
-    CUDA_TRY((launch_phi_batch<T, S>(d, nullptr, phi_blocks_of(h, h->phi_per_thread), st)));
+    CUDA_TRY((launch_phi_kernel<T, S>(h->paired, d, nullptr, phi_blocks_of(h, h->phi_per_thread), st)));
     if (mid) CUDA_TRY(cudaEventRecord(mid, st));
     if (gmu) {
       State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
       CUDA_TRY((launch_mu<T, S>(consts_of<T>(*h), s, st)));
     }
-    CUDA_TRY((launch_update_batch<T, S>(d, nullptr, upd_blocks_of(h), omega1_of(h), st, gmu)));
+    CUDA_TRY((launch_update_kernel<T, S>(h->paired, d, nullptr, upd_blocks_of(h), omega1_of(h), st, gmu)));
     return LBM_OK;
   }
   State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
@@ -607,6 +637,10 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   h->nz = nz;
   h->N = N;
   h->Np = Np;
+  // the linear layout by default: on the 150x150x107 ridge case the paired
+  // kernels executed fewer instructions per node but were slower (float32
+  // 0.1795 against 0.1699 ms per step, float16 0.1697 against 0.1667)
+  h->paired = false;
   h->tsize = precision == LBM_F64 ? 8 : 4;
   h->psize = precision == LBM_F64 ? 8 : (precision == LBM_F16 ? 2 : 4);
   h->wetting = params->theta_eq != 90.0 && params->kappa > 0;
@@ -658,18 +692,26 @@ int lbm_destroy(LbmHandle* h) {
   return LBM_OK;
 }
 
-int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, int fraction_dtype) {
-  NvtxRange range("lbm_set_geometry");
-  if (!h || !solid) return fail(LBM_E_ARG, "lbm_set_geometry: null argument");
-  if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
-    return fail(LBM_E_ARG, "lbm_set_geometry: fraction and fraction_dtype disagree");
-  compute_geometry(h->nx, h->ny, h->nz, solid, fraction, fraction_dtype, h->wetting, h->prec == LBM_F64, h->geo);
+namespace {
+// The device geometry precompute of a handle from device copies of the
+// solid mask and fraction, then the constant tables; asynchronous on `st`.
+// scratch: 2 N device bytes the kernels may use.
+int set_geometry_device(LbmHandle* h, const uint8_t* solid, const void* fraction, int fraction_dtype,
+                        uint8_t* scratch, cudaStream_t st) {
   const int64_t N = h->N;
-  CUDA_TRY(cudaMemcpy(h->cls, h->geo.cls.data(), N, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(h->wn, h->geo.wall_normal.data(), 3 * N * sizeof(float), cudaMemcpyHostToDevice));
-  if (h->prm.direct_wetting && h->wetting && h->prm.boundary_relax > 0) {
-    if (!h->nsw) CUDA_TRY(cudaMalloc(&h->nsw, N * sizeof(int)));
-    CUDA_TRY(cudaMemcpy(h->nsw, h->geo.nsw.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  const bool direct = h->prm.direct_wetting && h->wetting && h->prm.boundary_relax > 0;
+  if (direct && !h->nsw) CUDA_TRY(cudaMalloc(&h->nsw, N * sizeof(int)));
+  cudaError_t e;
+  if (h->prec == LBM_F64)
+    e = launch_geometry<double>((int)h->nx, (int)h->ny, (int)h->nz, solid, fraction, fraction_dtype, h->wetting,
+                                true, scratch, h->cls, h->wn, direct ? h->nsw : nullptr,
+                                static_cast<double*>(h->eps), st);
+  else
+    e = launch_geometry<float>((int)h->nx, (int)h->ny, (int)h->nz, solid, fraction, fraction_dtype, h->wetting,
+                               false, scratch, h->cls, h->wn, direct ? h->nsw : nullptr, static_cast<float*>(h->eps),
+                               st);
+  if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_set_geometry: ") + cudaGetErrorString(e));
+  if (direct) {
     if (!h->cubic) CUDA_TRY(cudaMalloc(&h->cubic, 4 * sizeof(double)));
     if (h->prec == LBM_F64) {
       double c4[4];
@@ -681,31 +723,55 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
       CUDA_TRY(cudaMemcpy(h->cubic, c4, sizeof(c4), cudaMemcpyHostToDevice));
     }
   }
-  // the penalisation fraction in the compute type: the caller's array itself
-  // when its type matches, else converted; zero without a fraction
-  const size_t ts = h->prec == LBM_F64 ? sizeof(double) : sizeof(float);
-  if (fraction_dtype == 0) {
-    CUDA_TRY(cudaMemset(h->eps, 0, N * ts));
-  } else if ((fraction_dtype == 1) == (h->prec != LBM_F64)) {
-    CUDA_TRY(cudaMemcpy(h->eps, fraction, N * ts, cudaMemcpyHostToDevice));
-  } else if (h->prec != LBM_F64) {
-    std::vector<float> eps(N);
-    for (int64_t n = 0; n < N; ++n) eps[n] = (float)static_cast<const double*>(fraction)[n];
-    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * ts, cudaMemcpyHostToDevice));
-  } else {
-    std::vector<double> eps(N);
-    for (int64_t n = 0; n < N; ++n) eps[n] = (double)static_cast<const float*>(fraction)[n];
-    CUDA_TRY(cudaMemcpy(h->eps, eps.data(), N * ts, cudaMemcpyHostToDevice));
-  }
   float lut[kWwCodes];
   near_wall_weights(lut);
   h->kf = make_consts<float>(*h, lut);
   h->kd = make_consts<double>(*h, lut);
   if (!lattice_table_matches(h->kf) || !lattice_table_matches(h->kd))
     return fail(LBM_E_ARG, "lbm_set_geometry: internal error: lattice constant table differs from the kernels' immediates");
+  h->cls_host.clear();
   h->geometry_set = true;
   h->desc_ok = false;
   return LBM_OK;
+}
+
+// The node-class table on the host (fetched once per geometry).
+int class_table_host(LbmHandle* h) {
+  if (!h->cls_host.empty()) return LBM_OK;
+  h->cls_host.resize((size_t)h->N);
+  CUDA_TRY(cudaMemcpy(h->cls_host.data(), h->cls, (size_t)h->N, cudaMemcpyDeviceToHost));
+  return LBM_OK;
+}
+}  // namespace
+
+int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, int fraction_dtype) {
+  NvtxRange range("lbm_set_geometry");
+  if (!h || !solid) return fail(LBM_E_ARG, "lbm_set_geometry: null argument");
+  if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
+    return fail(LBM_E_ARG, "lbm_set_geometry: fraction and fraction_dtype disagree");
+  // the inputs are staged through the population buffer the next step
+  // writes (it holds no state between steps): solid (N bytes), the fraction
+  // (N elements), then the kernels' 2 N bytes of scratch
+  const size_t N = (size_t)h->N;
+  const size_t fb = fraction_dtype == 0 ? 0 : N * (fraction_dtype == 1 ? 4 : 8);
+  uint8_t* stage = static_cast<uint8_t*>(h->f[h->cur ^ 1]);
+  const size_t off_f = (N + 255) & ~(size_t)255, off_s = (off_f + fb + 255) & ~(size_t)255;
+  CUDA_TRY(cudaMemcpyAsync(stage, solid, N, cudaMemcpyHostToDevice, 0));
+  if (fb) CUDA_TRY(cudaMemcpyAsync(stage + off_f, fraction, fb, cudaMemcpyHostToDevice, 0));
+  const int rc = set_geometry_device(h, stage, fb ? stage + off_f : nullptr, fraction_dtype, stage + off_s, 0);
+  if (rc != LBM_OK) return rc;
+  CUDA_TRY(cudaStreamSynchronize(0));
+  return LBM_OK;
+}
+
+int lbm_set_geometry_device(LbmHandle* h, const uint8_t* solid, const void* fraction, int fraction_dtype,
+                            void* stream) {
+  NvtxRange range("lbm_set_geometry_device");
+  if (!h || !solid) return fail(LBM_E_ARG, "lbm_set_geometry_device: null argument");
+  if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
+    return fail(LBM_E_ARG, "lbm_set_geometry_device: fraction and fraction_dtype disagree");
+  return set_geometry_device(h, solid, fraction, fraction_dtype, static_cast<uint8_t*>(h->f[h->cur ^ 1]),
+                             static_cast<cudaStream_t>(stream));
 }
 
 int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype) {
@@ -881,7 +947,8 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
   int rc = LBM_OK;
   for (const Tiling& t : cands) {
     // the two-kernel step: also its phi kernel's nodes per thread
-    const std::vector<int> pers = t.tx == 0 ? std::vector<int>{4, 8, 16, 32} : std::vector<int>{h->phi_per_thread};
+    const std::vector<int> pers =
+        t.tx == 0 ? std::vector<int>{4, 8, 12, 16, 24, 32} : std::vector<int>{h->phi_per_thread};
     for (int per : pers) {
       if (per != h->phi_per_thread) {
         h->phi_per_thread = per;
@@ -917,6 +984,26 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
     best_txyz3[2] = best.tz;
   }
   if (best_ms) *best_ms = best_t / reps;
+  return LBM_OK;
+}
+
+int lbm_set_layout(LbmHandle* h, int paired) {
+  if (!h) return fail(LBM_E_ARG, "lbm_set_layout: null handle");
+  if (paired != 0 && paired != 1) return fail(LBM_E_ARG, "lbm_set_layout: paired must be 0 or 1");
+  if (h->initialized) return fail(LBM_E_STATE, "lbm_set_layout: call before lbm_init_fields");
+  if (paired && (is2d(h) || h->nx % 2 != 0 || h->prec == LBM_F64))
+    return fail(LBM_E_UNSUPPORTED, "lbm_set_layout: the paired layout needs a 3-D grid with even nx in LBM_F32 or "
+                                   "LBM_F16");
+  h->paired = paired != 0;
+  h->kf.nh = h->paired ? (int)(h->N / 2) : 0;
+  h->kf.hx = h->paired ? (int)(h->nx / 2) : 0;
+  h->desc_ok = false;
+  return LBM_OK;
+}
+
+int lbm_get_layout(LbmHandle* h, int* paired) {
+  if (!h || !paired) return fail(LBM_E_ARG, "lbm_get_layout: null argument");
+  *paired = h->paired ? 1 : 0;
   return LBM_OK;
 }
 
@@ -1046,12 +1133,26 @@ int lbm_get_geometry(LbmHandle* h, uint8_t* node_class, uint8_t* is_boundary, fl
   if (!h) return fail(LBM_E_ARG, "lbm_get_geometry: null handle");
   if (!h->geometry_set) return fail(LBM_E_STATE, "lbm_get_geometry: no geometry");
   const size_t N = (size_t)h->N;
-  if (node_class) std::memcpy(node_class, h->geo.cls.data(), N);
-  if (is_boundary) std::memcpy(is_boundary, h->geo.boundary.data(), N);
-  if (wall_normal) std::memcpy(wall_normal, h->geo.wall_normal.data(), ndim_of(h->nz) * N * sizeof(float));
-  if (wall_weight) std::memcpy(wall_weight, h->geo.wall_weight.data(), N * sizeof(float));
-  if (near_wall) std::memcpy(near_wall, h->geo.near_wall.data(), N);
-  if (partial) std::memcpy(partial, h->geo.partial.data(), N);
+  // the device tables: the class byte carries the solid / boundary / partial
+  // bits and the near-wall distance code, from which the other tables follow
+  CUDA_TRY(cudaDeviceSynchronize());
+  const int rc = class_table_host(h);
+  if (rc != LBM_OK) return rc;
+  const uint8_t* c = h->cls_host.data();
+  if (node_class) std::memcpy(node_class, c, N);
+  if (wall_normal) CUDA_TRY(cudaMemcpy(wall_normal, h->wn, ndim_of(h->nz) * N * sizeof(float), cudaMemcpyDeviceToHost));
+  float lut[kWwCodes];
+  near_wall_weights(lut);
+  for (size_t n = 0; n < N; ++n) {
+    const uint8_t v = c[n];
+    const int code = v >> kWwShift;
+    if (is_boundary) is_boundary[n] = (v & kBoundary) ? 1 : 0;
+    if (partial) partial[n] = (v & kPartial) ? 1 : 0;
+    // weight exp(-d / 2.5) of the near-wall distance, 0 in solid and
+    // everywhere without wetting; near-wall where d < 10 (fe_wetting.py:295-303)
+    if (wall_weight) wall_weight[n] = h->wetting ? lut[code] : 0.0f;
+    if (near_wall) near_wall[n] = (!(v & kSolid) && code < 10) ? 1 : 0;
+  }
   return LBM_OK;
 }
 
@@ -1139,7 +1240,7 @@ struct StateHeader {
   int64_t steps;
   uint64_t geometry_hash;  // FNV-1a of the node-class table (the geometry the state belongs to)
   uint32_t status;
-  uint32_t reserved;
+  uint32_t layout;  // 1: paired storage layout, 0: linear
 };
 
 uint64_t fnv1a(const uint8_t* p, size_t n) {
@@ -1201,7 +1302,12 @@ int lbm_save_state(LbmHandle* h, void* host, int64_t bytes, void* stream) {
   hd.last_raw_in = h->last_raw_in;
   hd.obs_init = h->obs_init;
   hd.steps = h->steps;
-  hd.geometry_hash = fnv1a(h->geo.cls.data(), h->geo.cls.size());
+  {
+    const int rc = class_table_host(h);
+    if (rc != LBM_OK) return rc;
+  }
+  hd.geometry_hash = fnv1a(h->cls_host.data(), h->cls_host.size());
+  hd.layout = h->paired ? 1u : 0u;
   CUDA_TRY(cudaMemcpyAsync(&hd.status, h->counters + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
   char* out = static_cast<char*>(host) + sizeof(StateHeader);
   for (const StatePart& p : state_parts(h)) {
@@ -1223,8 +1329,14 @@ int lbm_load_state(LbmHandle* h, const void* host, int64_t bytes, void* stream) 
     return fail(LBM_E_ARG, "lbm_load_state: not a state written by lbm_save_state (bad magic or version)");
   if (hd.nx != h->nx || hd.ny != h->ny || hd.nz != h->nz || hd.prec != h->prec)
     return fail(LBM_E_ARG, "lbm_load_state: the state belongs to a different grid or precision");
-  if (hd.geometry_hash != fnv1a(h->geo.cls.data(), h->geo.cls.size()))
+  {
+    const int rc = class_table_host(h);
+    if (rc != LBM_OK) return rc;
+  }
+  if (hd.geometry_hash != fnv1a(h->cls_host.data(), h->cls_host.size()))
     return fail(LBM_E_ARG, "lbm_load_state: the state belongs to a different geometry");
+  if (hd.layout != (h->paired ? 1u : 0u))
+    return fail(LBM_E_ARG, "lbm_load_state: the state was written in the other storage layout (lbm_set_layout)");
   if (bytes != (int64_t)state_bytes(h)) return fail(LBM_E_ARG, "lbm_load_state: buffer size is not lbm_state_bytes");
   if ((hd.cur & ~1) || (hd.pc & ~1) || (hd.c_last & ~1) || hd.steps < 0)
     return fail(LBM_E_ARG, "lbm_load_state: corrupt header");
@@ -1266,13 +1378,13 @@ int lbm_reduce(LbmHandle* h, double* sum_phi, double* mom3, int32_t* extents6, f
     e = launch_measure<float>(nx, ny, nz, (const float*)h->meas_phi, h->cls, h->partials, kMeasureBlocks,
                               h->counters + 1, h->scal + 2, st, h->scal + 16);
     if (e == cudaSuccess)
-      e = launch_momentum<float>(N, (const float*)h->meas_phi, (const float*)h->u, us, h->prm.rho_l, h->prm.rho_g,
-                                 h->partials, kMeasureBlocks, h->counters + 4, h->scal + 24, st);
+      e = launch_momentum<float>(N, (const float*)h->meas_phi, (const float*)h->u, us, h->kf.nh, h->prm.rho_l,
+                                 h->prm.rho_g, h->partials, kMeasureBlocks, h->counters + 4, h->scal + 24, st);
   } else {
     e = launch_measure<double>(nx, ny, nz, (const double*)h->meas_phi, h->cls, h->partials, kMeasureBlocks,
                                h->counters + 1, h->scal + 2, st, h->scal + 16);
     if (e == cudaSuccess)
-      e = launch_momentum<double>(N, (const double*)h->meas_phi, (const double*)h->u, us, h->prm.rho_l,
+      e = launch_momentum<double>(N, (const double*)h->meas_phi, (const double*)h->u, us, h->kd.nh, h->prm.rho_l,
                                   h->prm.rho_g, h->partials, kMeasureBlocks, h->counters + 4, h->scal + 24, st);
   }
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_reduce: ") + cudaGetErrorString(e));
@@ -1328,19 +1440,25 @@ struct LbmBatch {
   std::vector<LbmHandle*> h;  // launch order: the cases with omega_f == 1 first
   int prec = LBM_F32;
   int device = 0;
-  int n_om1 = 0;            // cases [0, n_om1) have omega_f == 1
-  int phi_per_thread = 16;  // nodes per k_phi_batch thread
+  // cases in launch groups: [gstart[g], gstart[g + 1]) for g = 0 linear layout
+  // with omega_f == 1, 1 linear other, 2 paired layout with omega_f == 1, 3 paired other
+  int gstart[5] = {0, 0, 0, 0, 0};
+  int phi_per_thread = 16;  // nodes per phi-kernel thread (half as many pairs in the paired layout)
   size_t desc = 0;          // bytes of one case descriptor
   void* table[2] = {nullptr, nullptr};  // device descriptors: [0] this step, [1] the next
   unsigned char* staging = nullptr;     // pinned host copy of both tables
   cudaEvent_t staged = nullptr;         // the last copy out of `staging` has run
-  unsigned short* b2c = nullptr;        // block -> case: k_phi grid, then k_update (omega_f == 1, then other)
-  int phi_blocks = 0, upd_blocks[2] = {0, 0};
+  // block -> case: the phi grids of the linear and the paired cases, then the
+  // update grids of the four groups
+  unsigned short* b2c = nullptr;
+  int phi_blocks[2] = {0, 0}, upd_blocks[4] = {0, 0, 0, 0};
   cudaStream_t cap = nullptr;           // stream used to capture the two-step graph
   cudaGraphExec_t graph = nullptr;
 };
 
 namespace {
+
+int launch_group(const LbmHandle* h) { return (h->paired ? 2 : 0) + (omega1_of(h) ? 0 : 1); }
 
 // Block -> case tables (device) for the current phi_per_thread; drops the graph.
 int batch_layout(LbmBatch* b) {
@@ -1349,21 +1467,26 @@ int batch_layout(LbmBatch* b) {
   if (b->b2c) cudaFree(b->b2c);
   b->b2c = nullptr;
   const int n = (int)b->h.size();
-  long long pb = 0, ub[2] = {0, 0};
+  long long pb[2] = {0, 0}, ub[4] = {0, 0, 0, 0};
   for (int i = 0; i < n; ++i) {
-    pb += phi_blocks_of(b->h[i], b->phi_per_thread);
-    ub[i < b->n_om1 ? 0 : 1] += upd_blocks_of(b->h[i]);
+    pb[b->h[i]->paired ? 1 : 0] += phi_blocks_of(b->h[i], b->phi_per_thread);
+    ub[launch_group(b->h[i])] += upd_blocks_of(b->h[i]);
   }
-  if (pb > 0x7fffffff || ub[0] + ub[1] > 0x7fffffff) return fail(LBM_E_ARG, "lbm_batch: grids too large");
-  b->phi_blocks = (int)pb;
-  b->upd_blocks[0] = (int)ub[0];
-  b->upd_blocks[1] = (int)ub[1];
-  std::vector<unsigned short> t((size_t)(pb + ub[0] + ub[1]));
-  size_t at[3] = {0, (size_t)pb, (size_t)(pb + ub[0])};
+  const long long tot = pb[0] + pb[1] + ub[0] + ub[1] + ub[2] + ub[3];
+  if (tot > 0x7fffffff) return fail(LBM_E_ARG, "lbm_batch: grids too large");
+  for (int j = 0; j < 2; ++j) b->phi_blocks[j] = (int)pb[j];
+  for (int g = 0; g < 4; ++g) b->upd_blocks[g] = (int)ub[g];
+  std::vector<unsigned short> t((size_t)tot);
+  size_t at[6];
+  at[0] = 0;
+  at[1] = (size_t)pb[0];
+  at[2] = at[1] + (size_t)pb[1];
+  for (int g = 0; g < 3; ++g) at[3 + g] = at[2 + g] + (size_t)ub[g];
   for (int i = 0; i < n; ++i) {
-    for (int k = phi_blocks_of(b->h[i], b->phi_per_thread); k > 0; --k) t[at[0]++] = (unsigned short)i;
-    size_t& a = at[i < b->n_om1 ? 1 : 2];
-    for (int k = upd_blocks_of(b->h[i]); k > 0; --k) t[a++] = (unsigned short)i;
+    size_t& a = at[b->h[i]->paired ? 1 : 0];
+    for (int k = phi_blocks_of(b->h[i], b->phi_per_thread); k > 0; --k) t[a++] = (unsigned short)i;
+    size_t& c = at[2 + launch_group(b->h[i])];
+    for (int k = upd_blocks_of(b->h[i]); k > 0; --k) t[c++] = (unsigned short)i;
   }
   CUDA_TRY(cudaMalloc(&b->b2c, t.size() * sizeof(unsigned short)));
   CUDA_TRY(cudaMemcpy(b->b2c, t.data(), t.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
@@ -1374,18 +1497,19 @@ int batch_layout(LbmBatch* b) {
 template <typename T, typename S>
 void batch_fill_t(LbmBatch* b) {
   const int n = (int)b->h.size();
-  int pb = 0, ub[2] = {0, 0};
+  int pb[2] = {0, 0}, ub[4] = {0, 0, 0, 0};
   for (int i = 0; i < n; ++i) {
     LbmHandle* h = b->h[i];
-    const int phin = phi_blocks_of(h, b->phi_per_thread), updn = upd_blocks_of(h), g = i < b->n_om1 ? 0 : 1;
+    const int phin = phi_blocks_of(h, b->phi_per_thread), updn = upd_blocks_of(h), g = launch_group(h);
+    int& pbl = pb[h->paired ? 1 : 0];
     for (int par = 0; par < 2; ++par) {
       State<T, S> s = make_state<T, S>(*h, h->cur ^ par, h->pc ^ par);
       s.c_prev = h->c_last ^ par;
       s.c_cur = h->c_last ^ par ^ 1;
-      fill_case_desc<T, S>(b->staging + ((size_t)par * n + i) * b->desc, consts_of<T>(*h), s, pb, phin, ub[g],
+      fill_case_desc<T, S>(b->staging + ((size_t)par * n + i) * b->desc, consts_of<T>(*h), s, pbl, phin, ub[g],
                            updn);
     }
-    pb += phin;
+    pbl += phin;
     ub[g] += updn;
   }
 }
@@ -1404,16 +1528,21 @@ int batch_fill(LbmBatch* b, cudaStream_t st) {
   return LBM_OK;
 }
 
-// One batched step reading descriptor table `par`: k_phi over every case, then
-// k_update over the omega_f == 1 cases and over the others.
+// One batched step reading descriptor table `par`: the phi kernel over every
+// linear-layout case and over every paired case, then the update kernel over
+// each group (layout x omega_f == 1 or not).  Empty launches are skipped.
 template <typename T, typename S>
 cudaError_t batch_launch_t(LbmBatch* b, int par, cudaStream_t st) {
-  cudaError_t e = launch_phi_batch<T, S>(b->table[par], b->b2c, b->phi_blocks, st);
-  if (e == cudaSuccess)
-    e = launch_update_batch<T, S>(b->table[par], b->b2c + b->phi_blocks, b->upd_blocks[0], true, st);
-  if (e == cudaSuccess)
-    e = launch_update_batch<T, S>(b->table[par], b->b2c + b->phi_blocks + b->upd_blocks[0], b->upd_blocks[1],
-                                  false, st);
+  const unsigned short* t = b->b2c;
+  cudaError_t e = cudaSuccess;
+  for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+    e = launch_phi_kernel<T, S>(j == 1, b->table[par], t, b->phi_blocks[j], st);
+    t += b->phi_blocks[j];
+  }
+  for (int g = 0; g < 4 && e == cudaSuccess; ++g) {
+    e = launch_update_kernel<T, S>(g >= 2, b->table[par], t, b->upd_blocks[g], (g & 1) == 0, st, false);
+    t += b->upd_blocks[g];
+  }
   return e;
 }
 cudaError_t batch_launch(LbmBatch* b, int par, cudaStream_t st) {
@@ -1479,10 +1608,12 @@ int lbm_batch_create(LbmHandle* const* handles, int n, LbmBatch** out) {
   if (!b) return fail(LBM_E_ARG, "lbm_batch_create: out of host memory");
   b->prec = handles[0]->prec;
   b->device = dev;
-  for (int pass = 0; pass < 2; ++pass)
+  for (int g = 0; g < 4; ++g) {
+    b->gstart[g] = (int)b->h.size();
     for (int i = 0; i < n; ++i)
-      if (omega1_of(handles[i]) == (pass == 0)) b->h.push_back(handles[i]);
-  for (int i = 0; i < n; ++i) b->n_om1 += omega1_of(handles[i]) ? 1 : 0;
+      if (launch_group(handles[i]) == g) b->h.push_back(handles[i]);
+  }
+  b->gstart[4] = (int)b->h.size();
   b->desc = with_types(b->prec, [&](auto tag) {
     return case_desc_bytes<typename decltype(tag)::T, typename decltype(tag)::S>();
   });
@@ -1579,7 +1710,7 @@ int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread
   CUDA_TRY(cudaEventCreate(&e1));
   int best = b->phi_per_thread, rc = LBM_OK;
   float best_t = 1e30f;
-  for (int per : {1, 2, 4, 8, 16, 32}) {
+  for (int per : {1, 2, 4, 8, 12, 16, 24, 32}) {
     b->phi_per_thread = per;
     rc = batch_layout(b);
     if (rc == LBM_OK) rc = batch_fill(b, st);

@@ -7,7 +7,11 @@
 namespace lbm {
 
 constexpr int Q = 19;
-constexpr int kBlock = 256;  // threads per block of every node-parallel kernel
+constexpr int kBlock = 256;  // threads per block of the node-parallel kernels
+// Threads per block of the paired update kernel (lbm_pair.cuh): blocks of 128
+// threads at 128 registers (4 per SM) leave fewer SM slots idle behind a
+// block's last warp than blocks of 256 (2 per SM).
+constexpr int kPairUpdBlock = 128;
 
 // D3Q19 velocity set in the population order of the reference
 // (pytorch-lbm lbm/lattice.py:70-95).  Written as constexpr functions so that
@@ -125,8 +129,17 @@ inline FastDiv make_fastdiv(unsigned d) {
   return f;
 }
 
-// Population arrays (f, g) and u store component j of node n at j * Np + n,
-// Np = N rounded up to a multiple of kAlignNodes, so that every component
+// Storage element of node n (see Consts::nh): n in the linear layout, 2n or
+// 2(n - nh) + 1 in the paired layout.
+template <typename K>
+__host__ __device__ __forceinline__ unsigned sidx(const K& k, int n) {
+  const unsigned nh = (unsigned)k.nh, un = (unsigned)n;
+  if (nh == 0u) return un;
+  return un < nh ? 2u * un : 2u * (un - nh) + 1u;
+}
+
+// Population arrays (f, g), u and phi store component j of node n at
+// j * Np + sidx(n), Np = N rounded up to a multiple of kAlignNodes, so that every component
 // array starts on a 128-byte line and a warp's 32 consecutive nodes of one
 // component fill whole lines.  Caller-facing arrays are dense (j * N + n).
 constexpr int kAlignNodes = 32;
@@ -139,6 +152,15 @@ struct Consts {
   int nx, ny, nz, N;
   int Np;             // component stride of f, g and u (N rounded up to kAlignNodes)
   FastDiv dz, dy;     // division by nz and by ny
+  // Paired layout (3-D grids with even nx): nodes x and x + nx/2 of the same
+  // (y, z) share one pair p = ((x mod nx/2) ny + y) nz + z; the populations,
+  // u and phi of the pair's lower node sit at element 2p of their component
+  // array and the upper node's at 2p + 1, so one 8-byte (float) or 4-byte
+  // (half) word holds both.  nh = N / 2 pairs, hx = nx / 2; nh == 0 selects
+  // the linear layout (element n).  Node-indexed arrays (class byte, wall
+  // normal, fraction, amplification, mu) keep node order n: the lower node of
+  // pair p is node p, the upper node p + nh.
+  int nh, hx;
   T w[Q];      // lattice weights (float32 table, widened)
   T wc[Q];     // w_i / cs2                      (stencil weights)
   T w2c[Q];    // 2 w_i / cs2                    (laplacian weights)

@@ -234,21 +234,24 @@ __device__ __forceinline__ __half ldg(const __half* p) { return __ldg(p); }
 // f encoding of PopIO; phi_in (the previous step's phi) supplies the deviation
 // references of the half form: the node's own phi for pulled values, the
 // neighbour x - e_q's phi for the node's own opposite slot (bounce-back, VP).
-template <typename T, typename S, bool RAW, bool WITH_C, bool IS_F, bool USE_POL = false>
+// MAP: the state arrays use the layout of k (sidx); without it the linear
+// layout is assumed (the batched single-node kernels, which serve linear grids).
+template <typename T, typename S, bool RAW, bool WITH_C, bool IS_F, bool USE_POL = false, bool MAP = false>
 __device__ __forceinline__ void fetch_pop(T (&v)[Q], const Consts<T>& k, const S* __restrict__ F,
                                           const T* __restrict__ phi_in, int n, size_t N, const Nbr& nb,
                                           uint8_t c, T eps, T corr, unsigned long long pol = 0ull) {
   using IO = PopIO<T, S>;
+  auto I = [&](int m) -> unsigned { return MAP ? sidx(k, m) : (unsigned)m; };
   // element offsets q Np + m stay below 2^31 (checked when the grid is created)
-  const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+  const unsigned Nu = (unsigned)k.Np, nu = I(n);
   (void)N;
-  const T ref_self = (IO::kDev && IS_F) ? ldg(phi_in + n) : T(0);
+  const T ref_self = (IO::kDev && IS_F) ? ldg(phi_in + nu) : T(0);
   auto ld = [&](int q, unsigned idx, T ref) -> T {
     const S raw = ld_sel<USE_POL>(F + idx, pol);
     return IS_F ? IO::ld_f(raw, q, ref, k) : IO::ld_g(raw, q, k);
   };
   auto ref_nb = [&](int q) -> T {
-    return (IO::kDev && IS_F) ? ldg(phi_in + nb.at(n, -ex(q), -ey(q), -ez(q))) : T(0);
+    return (IO::kDev && IS_F) ? ldg(phi_in + I(nb.at(n, -ex(q), -ey(q), -ez(q)))) : T(0);
   };
   if (RAW) {
 #pragma unroll
@@ -260,7 +263,7 @@ __device__ __forceinline__ void fetch_pop(T (&v)[Q], const Consts<T>& k, const S
     for (int q = 0; q < Q; ++q) v[q] = ld(opp(q), opp(q) * Nu + nu, ref_nb(q));
   } else {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ld(q, q * Nu + (unsigned)nb.at(n, -ex(q), -ey(q), -ez(q)), ref_self);
+    for (int q = 0; q < Q; ++q) v[q] = ld(q, q * Nu + I(nb.at(n, -ex(q), -ey(q), -ez(q))), ref_self);
     if (c & kPartial) {
       const T one_m = T(1) - eps;
 #pragma unroll
@@ -287,7 +290,7 @@ __device__ __forceinline__ T seqsum(const T (&v)[Q]) {
 // direct wetting the target is the cubic-wall-energy boundary phi from the
 // corrected phi of the node's next-interior node (fe_wetting.py:369-416), or
 // the node's own phi where that does not apply.
-template <typename T>
+template <typename T, bool MAP = false>
 __device__ __forceinline__ T relax_target(const Consts<T>& k, const T* __restrict__ phi_arr,
                                           const int* __restrict__ nsw, const T* __restrict__ cubic, int n, T phi_prev,
                                           T corr) {
@@ -298,7 +301,7 @@ __device__ __forceinline__ T relax_target(const Consts<T>& k, const T* __restric
     target = pb;
     const int m = nsw[n];
     if (m >= 0 && cubic[3] != T(0) && pb > T(0.01) && pb < T(0.99)) {
-      const T pn = clamp01(phi_arr[m] * corr);
+      const T pn = clamp01(phi_arr[MAP ? sidx(k, m) : (unsigned)m] * corr);
       T disc = cubic[0] + cubic[1] * pn;
       disc = disc < T(0) ? T(0) : disc;
       target = clamp01((cubic[2] + sqrt(disc)) / cubic[3]);
@@ -316,13 +319,14 @@ __device__ __forceinline__ T relax_scale(T target, T sum_f) {
 }
 
 // f at node n as the reference holds it at the start of the step.
-template <typename T, typename S, bool RAW, bool USE_POL = false>
+template <typename T, typename S, bool RAW, bool USE_POL = false, bool MAP = false>
 __device__ __forceinline__ void fetch_f(T (&v)[Q], const Consts<T>& k, const State<T, S>& s, int n, size_t N,
                                         const Nbr& nb, uint8_t c, T eps, unsigned long long pol = 0ull) {
   const T corr = RAW ? T(1) : s.cbuf[s.c_prev];
-  fetch_pop<T, S, RAW, !RAW, true, USE_POL>(v, k, s.fin, s.phi_in, n, N, nb, c, eps, corr, pol);
+  fetch_pop<T, S, RAW, !RAW, true, USE_POL, MAP>(v, k, s.fin, s.phi_in, n, N, nb, c, eps, corr, pol);
   if (!RAW && k.relax_on && (c & kTop)) {
-    const T r = relax_target(k, s.phi_in, s.nsw, s.cubic, n, ldg(s.phi_in + n), corr);
+    const T r = relax_target<T, MAP>(k, s.phi_in, s.nsw, s.cubic, n,
+                                     ldg(s.phi_in + (MAP ? sidx(k, n) : (unsigned)n)), corr);
     if (r >= T(0)) {
       const T sc = relax_scale(r, seqsum(v));
 #pragma unroll
@@ -487,14 +491,14 @@ constexpr int kStage = Q + 4;
 template <typename T, bool RAW, bool FIRST>
 __device__ __forceinline__ void stage_node(const Consts<T>& k, const State<T, T>& s, int n, const Nbr& nb,
                                            T* st, unsigned long long pol) {
-  const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+  const unsigned Nu = (unsigned)k.Np, nu = sidx(k, n);
   if (RAW) {
 #pragma unroll
     for (int q = 0; q < Q; ++q) cp_async(st + q * kBlock, s.gin + (q * Nu + nu), pol);
   } else {
 #pragma unroll
     for (int q = 0; q < Q; ++q)
-      cp_async(st + q * kBlock, s.gin + (q * Nu + (unsigned)nb.at(n, -ex(q), -ey(q), -ez(q))), pol);
+      cp_async(st + q * kBlock, s.gin + (q * Nu + sidx(k, nb.at(n, -ex(q), -ey(q), -ez(q)))), pol);
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) cp_async(st + (Q + d) * kBlock, s.u + (d * Nu + nu), pol);
@@ -504,7 +508,7 @@ __device__ __forceinline__ void stage_node(const Consts<T>& k, const State<T, T>
 // STAGED: g, u and the previous phi come from the node's cp.async staging
 // slot `st` (word j at st[j * kBlock]); otherwise they are loaded here.
 template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool STAGED, bool STORE_PHI, bool GMU,
-          typename PhiAt, typename SolidAt, typename RefAt>
+          bool MAP, typename PhiAt, typename SolidAt, typename RefAt>
 __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S>& s, int n, const Nbr& nb,
                                             uint8_t c, T phi, PhiAt phi_at, SolidAt solid_at, RefAt ref_at,
                                             const Pol& pol, const T* st) {
@@ -512,7 +516,8 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   constexpr bool IMM = IO::kDev;
   const LatK<T, IMM> L{k};
   const size_t N = (size_t)k.N;
-  const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+  // nu: the node's storage element (f, g, u, phi); nn: its node index (node-order arrays)
+  const unsigned Nu = (unsigned)k.Np, nu = MAP ? sidx(k, n) : (unsigned)n, nn = (unsigned)n;
 
   // 2. first the stencil: gradient and laplacian with the ghost-node wetting values
   T ps[Q];
@@ -549,11 +554,11 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     uo2 = st[(Q + 2) * kBlock];
     pp = FIRST ? T(0) : st[(Q + 3) * kBlock];
   } else {
-    fetch_pop<T, S, RAW, false, false, true>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1), pol.once);
+    fetch_pop<T, S, RAW, false, false, true, MAP>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1), pol.once);
     uo0 = ld_pol(s.u + nu, pol.once);
     uo1 = ld_pol(s.u + (Nu + nu), pol.once);
     uo2 = ld_pol(s.u + (2 * Nu + nu), pol.once);
-    pp = FIRST ? T(0) : ld_pol(s.phi_in + n, pol.once);
+    pp = FIRST ? T(0) : ld_pol(s.phi_in + nu, pol.once);
   }
 
   const T rho = fma_(phi, k.rho_l, (T(1) - phi) * k.rho_g);
@@ -663,8 +668,8 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
     if (k.wetting) cl = cl * (T(1) - k.sharpen_reduce * k.ww[c >> kWwShift]);
     if constexpr (GMU) {
       // grad mu of this node (k_gradmu)
-      const T mx = ld_pol(s.gmu + nu, pol.once), my = ld_pol(s.gmu + (Nu + nu), pol.once),
-              mz = ld_pol(s.gmu + (2 * Nu + nu), pol.once);
+      const T mx = ld_pol(s.gmu + nn, pol.once), my = ld_pol(s.gmu + (Nu + nn), pol.once),
+              mz = ld_pol(s.gmu + (2 * Nu + nn), pol.once);
       if (k.gmu_mode == kGmuCH) {
         // Cahn-Hilliard: d(phi u) + M (grad mu - grad phi) tau_f / (tau_f - 1/2)  (:457-461)
         S0 = d0 + (k.mob * (mx - gx)) * k.guo;
@@ -704,7 +709,7 @@ __device__ __forceinline__ void update_node(const Consts<T>& k, const State<T, S
   const T pf = OMEGA1 ? phi : k.omega_f * phi;  // omega_f phi
   const T u3x = u0 * L.inv_cs2(), u3y = u1 * L.inv_cs2(), u3z = u2 * L.inv_cs2();
   T f[Q];
-  if (!OMEGA1) fetch_f<T, S, RAW, true>(f, k, s, n, N, nb, c, eps, pol.same);
+  if (!OMEGA1) fetch_f<T, S, RAW, true, MAP>(f, k, s, n, N, nb, c, eps, pol.same);
   auto store_g = [&](int q, T v) { st_pol(s.gout + (q * Nu + nu), IO::st_g(v, q, k), pol.once); };
   auto store_f = [&](int q, T v) {
     st_pol(s.fout + (q * Nu + nu), IO::st_f(v, q, IO::kDev ? ref_at(q) : T(0), k), pol.once);
@@ -927,7 +932,7 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
       if (!(c & kSolid)) {
         const T eps = (c & kPartial) ? s.eps[n] : T(0);
         T v[Q];
-        fetch_f<T, S, RAW, true>(v, k, s, n, N, nbc, c, eps, pol.keep);
+        fetch_f<T, S, RAW, true, true>(v, k, s, n, N, nbc, c, eps, pol.keep);
         phi = clamp01(seqsum(v));
       }
       sphi[h] = phi;
@@ -952,7 +957,7 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
         const Nbr nb = make_nbr_xyz(gx, gy, gz, k.nx, k.ny, k.nz);
         const T eps = (c & kPartial) ? s.eps[n] : T(0);
         T v[Q];
-        fetch_f<T, S, RAW, true>(v, k, s, n, N, nb, c, eps, pol.keep);
+        fetch_f<T, S, RAW, true, true>(v, k, s, n, N, nb, c, eps, pol.keep);
         phi = clamp01(seqsum(v));
       }
       sphi[h] = phi;
@@ -998,7 +1003,7 @@ __global__ void __launch_bounds__(kBlock, StepOccupancy<T, S>::blocks) k_step(Co
       const Nbr nb = make_nbr_xyz(x0 + lx, y0 + ly, z0 + lz, k.nx, k.ny, k.nz);
       // phi of this step at x + e_q (also the deviation reference, in the half
       // form, of the next step's reader of slot (x, q))
-      update_node<T, S, RAW, FIRST, OMEGA1, STAGED, true, false>(
+      update_node<T, S, RAW, FIRST, OMEGA1, STAGED, true, false, true>(
           k, s, n, nb, scls[h], sphi[h], [&](int q) { return sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)]; },
           [&](int q) { return (scls[h + ex(q) * sx + ey(q) * HZ + ez(q)] & kSolid) != 0; },
           [&](int q) { return sphi[h + ex(q) * sx + ey(q) * HZ + ez(q)]; }, pol,
@@ -1027,7 +1032,7 @@ __device__ __forceinline__ void decode(const FastDiv& dz, const FastDiv& dy, int
 // Persistent: a grid of about one wave strides over the nodes, so that the
 // per-block publication of the partial sum happens once per block.
 // phi of node n (written to phi_out) added to the block's sum.
-template <typename T, typename S, bool RAW>
+template <typename T, typename S, bool RAW, bool MAP = false>
 __device__ __forceinline__ void phi_node(const Consts<T>& k, const State<T, S>& s, int n, uint8_t c, const Pol& pol,
                                          TileSum<T>& part) {
   T phi = T(0);
@@ -1038,10 +1043,10 @@ __device__ __forceinline__ void phi_node(const Consts<T>& k, const State<T, S>& 
     const T eps = (c & kPartial) ? s.eps[n] : T(0);
     T v[Q];
     // f is read again by k_update only when omega_f != 1
-    fetch_f<T, S, RAW, true>(v, k, s, n, (size_t)k.N, nb, c, eps, k.omega_f == T(1) ? pol.once : pol.keep);
+    fetch_f<T, S, RAW, true, MAP>(v, k, s, n, (size_t)k.N, nb, c, eps, k.omega_f == T(1) ? pol.once : pol.keep);
     phi = clamp01(seqsum(v));
   }
-  st_pol(s.phi_out + n, phi, pol.keep);  // read back (stencil) by k_update
+  st_pol(s.phi_out + (MAP ? sidx(k, n) : (unsigned)n), phi, pol.keep);  // read back (stencil) by k_update
   part.add(phi);
 }
 
@@ -1070,7 +1075,7 @@ __global__ void __launch_bounds__(kBlock) k_phi(Consts<T> k, State<T, S> s) {
   const Pol pol = Pol::make();
   TileSum<T> part;
   for (int n = blockIdx.x * kBlock + threadIdx.x; n < k.N; n += gridDim.x * kBlock)
-    phi_node<T, S, RAW>(k, s, n, s.cls[n], pol, part);
+    phi_node<T, S, RAW, true>(k, s, n, s.cls[n], pol, part);
   phi_finish(s, part, blockIdx.x, gridDim.x);
 }
 
@@ -1082,18 +1087,19 @@ struct UpdateOccupancy {
   static constexpr int blocks = sizeof(T) == 8 ? 1 : 4;
 };
 
-template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool GMU>
+template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool GMU, bool MAP = false>
 __device__ __forceinline__ void update_one(const Consts<T>& k, const State<T, S>& s, int n, const Pol& pol) {
   int ix, iy, iz;
   decode(k.dz, k.dy, n, k.nz, k.ny, ix, iy, iz);
   const Nbr nb = make_nbr_xyz(ix, iy, iz, k.nx, k.ny, k.nz);
   const T* __restrict__ pc = s.phi_out;  // phi of this step (k_phi)
   const uint8_t c = s.cls[n];
-  const T phi = ld_pol(pc + n, pol.keep);
-  update_node<T, S, RAW, FIRST, OMEGA1, false, false, GMU>(
-      k, s, n, nb, c, phi, [&](int q) { return ld_pol(pc + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); },
+  auto I = [&](int m) -> unsigned { return MAP ? sidx(k, m) : (unsigned)m; };
+  const T phi = ld_pol(pc + I(n), pol.keep);
+  update_node<T, S, RAW, FIRST, OMEGA1, false, false, GMU, MAP>(
+      k, s, n, nb, c, phi, [&](int q) { return ld_pol(pc + I(nb.at(n, ex(q), ey(q), ez(q))), pol.keep); },
       [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; },
-      [&](int q) { return ld_pol(pc + nb.at(n, ex(q), ey(q), ez(q)), pol.keep); }, pol, (const T*)nullptr);
+      [&](int q) { return ld_pol(pc + I(nb.at(n, ex(q), ey(q), ez(q))), pol.keep); }, pol, (const T*)nullptr);
 }
 
 // One thread per node, linear order.  (Measured slower on the 150x150x107
@@ -1104,7 +1110,7 @@ __device__ __forceinline__ void update_one(const Consts<T>& k, const State<T, S>
 template <typename T, typename S, bool RAW, bool FIRST, bool OMEGA1, bool GMU = false>
 __global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S, GMU>::blocks) k_update(Consts<T> k, State<T, S> s) {
   const int n = blockIdx.x * kBlock + threadIdx.x;
-  if (n < k.N) update_one<T, S, RAW, FIRST, OMEGA1, GMU>(k, s, n, Pol::make());
+  if (n < k.N) update_one<T, S, RAW, FIRST, OMEGA1, GMU, true>(k, s, n, Pol::make());
 }
 
 // Gradient of the chemical potential of every node (mu from k_mu), for the
@@ -1141,10 +1147,10 @@ __global__ void __launch_bounds__(kBlock) k_mu(Consts<T> k, State<T, S> s) {
   const Pol pol = Pol::make();
   const T* __restrict__ pc = s.phi_out;
   const uint8_t c = s.cls[n];
-  const T phi = ld_pol(pc + n, pol.keep);
+  const T phi = ld_pol(pc + sidx(k, n), pol.keep);
   T ps[Q];
 #pragma unroll
-  for (int q = 1; q < Q; ++q) ps[q] = ld_pol(pc + nb.at(n, ex(q), ey(q), ez(q)), pol.keep);
+  for (int q = 1; q < Q; ++q) ps[q] = ld_pol(pc + sidx(k, nb.at(n, ex(q), ey(q), ez(q))), pol.keep);
   auto solid_at = [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; };
   T gx, gy, gz, lap;
   grad_lap<T, true, State<T, S>, decltype(solid_at), true>(k, s, n, c, phi, ps, solid_at, gx, gy, gz, lap);
@@ -1221,6 +1227,12 @@ __global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S, GMU>::blocks) k_
   if (n < d.k.N) update_one<T, S, false, false, OMEGA1, GMU>(d.k, d.s, n, Pol::make());
 }
 
+}  // namespace lbm
+
+#include "lbm_pair.cuh"
+
+namespace lbm {
+
 // Grid of a persistent kernel: resident blocks per SM x SMs (one wave), at
 // most one block per kBlock nodes.  The occupancy lookup runs once per kernel
 // and device; host threads may launch concurrently (the serving loop sets up
@@ -1267,17 +1279,18 @@ __global__ void __launch_bounds__(kBlock) k_init(Consts<T> k, State<T, S> s, con
     const T b = ((v0 * v0 + v1 * v1) + v2 * v2) / k.two_cs2;
     S* f = const_cast<S*>(s.fin);
     S* g = const_cast<S*>(s.gin);
+    const unsigned e = sidx(k, n);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const T ec = edot(q, v0, v1, v2) / k.cs2;
       // the state right after init is read in place (RAW): deviation reference = own phi
-      f[(size_t)q * k.Np + n] = IO::st_f(phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b)), q, phi, k);
-      g[(size_t)q * k.Np + n] = IO::st_g(T(0) * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b), q, k);
+      f[(size_t)q * k.Np + e] = IO::st_f(phi * (k.w[q] * (((T(1) + ec) + ec * ec / T(2)) - b)), q, phi, k);
+      g[(size_t)q * k.Np + e] = IO::st_g(T(0) * k.w[q] + k.w[q] * ((ec + ec * ec / T(2)) - b), q, k);
     }
-    s.u[n] = v0;
-    s.u[k.Np + n] = v1;
-    s.u[2 * (size_t)k.Np + n] = v2;
-    s.phi_out[n] = phi;
+    s.u[e] = v0;
+    s.u[k.Np + e] = v1;
+    s.u[2 * (size_t)k.Np + e] = v2;
+    s.phi_out[e] = phi;
     part = (double)phi;
   }
   part = block_sum(part);
@@ -1308,7 +1321,7 @@ __global__ void __launch_bounds__(kBlock) k_inject(Consts<T> k, State<T, S> s, I
   bool core = false;
   if (n < k.N) {
     const size_t N = (size_t)k.N;
-    const unsigned Nu = (unsigned)k.Np, nu = (unsigned)n;
+    const unsigned Nu = (unsigned)k.Np, nu = sidx(k, n);
     const uint8_t c = s.cls[n];
     int ix, iy, iz;
     const Nbr nb = make_nbr(n, k.nx, k.ny, k.nz, &ix, &iy, &iz);
@@ -1321,12 +1334,12 @@ __global__ void __launch_bounds__(kBlock) k_inject(Consts<T> k, State<T, S> s, I
     core = C > T(0.1);
     // the attributes phi, u, P the reference holds now
     const T corr = s.cbuf[s.c_prev];
-    T phi = s.phi_in[n];
+    T phi = s.phi_in[nu];
     if (!ip.obs_init) {
       const T pr = phi;
       phi = clamp01(pr * corr);
       if (k.relax_on && (c & kTop)) {
-        const T r = relax_target(k, s.phi_in, s.nsw, s.cubic, n, pr, corr);
+        const T r = relax_target<T, true>(k, s.phi_in, s.nsw, s.cubic, n, pr, corr);
         if (r >= T(0)) phi = r;
       }
     }
@@ -1335,8 +1348,8 @@ __global__ void __launch_bounds__(kBlock) k_inject(Consts<T> k, State<T, S> s, I
     // the populations the reference holds now
     const T eps = (c & kPartial) ? s.eps[n] : T(0);
     T fv[Q], gv[Q];
-    fetch_f<T, S, RAW>(fv, k, s, n, N, nb, c, eps);
-    fetch_pop<T, S, RAW, false, false>(gv, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
+    fetch_f<T, S, RAW, false, true>(fv, k, s, n, N, nb, c, eps);
+    fetch_pop<T, S, RAW, false, false, false, true>(gv, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
     // new phi: the maximum with the droplet in its core, clamped, zero in solid
     T pn = core ? (phi > C ? phi : C) : phi;
     pn = clamp01(pn);
@@ -1365,7 +1378,7 @@ __global__ void __launch_bounds__(kBlock) k_inject(Consts<T> k, State<T, S> s, I
     s.u[nu] = u[0];
     s.u[Nu + nu] = u[1];
     s.u[2 * Nu + nu] = u[2];
-    s.phi_out[n] = pn;
+    s.phi_out[nu] = pn;
     part = (double)pn;
   }
   const int cnt = __syncthreads_count(core);
@@ -1391,7 +1404,8 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
   if (n >= k.N) return;
   const size_t N = (size_t)k.N;
   const uint8_t c = s.cls[n];
-  const T phi = s.phi_out[n];
+  const unsigned e = sidx(k, n);
+  const T phi = s.phi_out[e];
   const T rho = phi * k.rho_l + (T(1) - phi) * k.rho_g;
   if (mask & 1u) {
     T v = phi;
@@ -1399,7 +1413,7 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
       const T corr = s.cbuf[s.c_cur];
       v = clamp01(phi * corr);
       if (k.relax_on && (c & kTop)) {
-        const T r = relax_target(k, (const T*)s.phi_out, s.nsw, s.cubic, n, phi, corr);
+        const T r = relax_target<T, true>(k, (const T*)s.phi_out, s.nsw, s.cubic, n, phi, corr);
         if (r >= T(0)) v = r;
       }
     }
@@ -1407,9 +1421,9 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
   }
   if (mask & 2u) rho_o[n] = rho;
   if (mask & 4u) {
-    u_o[n] = s.u[n];
-    u_o[N + n] = s.u[k.Np + n];
-    u_o[2 * N + n] = s.u[2 * (size_t)k.Np + n];
+    u_o[n] = s.u[e];
+    u_o[N + n] = s.u[k.Np + e];
+    u_o[2 * N + n] = s.u[2 * (size_t)k.Np + e];
   }
   if (mask & (8u | 16u | 32u)) {
     int ix, iy, iz;
@@ -1419,7 +1433,7 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
       if (mode == kObsStep) {
         const T eps = (c & kPartial) ? s.eps[n] : T(0);
         T g[Q];
-        fetch_pop<T, S, RAW_IN, false, false>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
+        fetch_pop<T, S, RAW_IN, false, false, false, true>(g, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
         P = seqsum(g);
       }
       if (mask & 8u) P_o[n] = P;
@@ -1428,7 +1442,7 @@ __global__ void __launch_bounds__(kBlock) k_observe(Consts<T> k, State<T, S> s, 
     if (mask & 32u) {
       T ps[Q];
 #pragma unroll
-      for (int q = 1; q < Q; ++q) ps[q] = ldg(s.phi_out + nb.at(n, ex(q), ey(q), ez(q)));
+      for (int q = 1; q < Q; ++q) ps[q] = ldg(s.phi_out + sidx(k, nb.at(n, ex(q), ey(q), ez(q))));
       auto nsolid = [&](int q) { return (s.cls[nb.at(n, ex(q), ey(q), ez(q))] & kSolid) != 0; };
       T gx, gy, gz, lap;
       if (mode == kObsStep) grad_lap<T, true>(k, s, n, c, phi, ps, nsolid, gx, gy, gz, lap);
@@ -1451,12 +1465,12 @@ __global__ void __launch_bounds__(kBlock) k_populations(Consts<T> k, State<T, S>
   const T eps = (c & kPartial) ? s.eps[n] : T(0);
   T v[Q];
   if (f_o) {
-    fetch_f<T, S, RAW>(v, k, s, n, N, nb, c, eps);
+    fetch_f<T, S, RAW, false, true>(v, k, s, n, N, nb, c, eps);
 #pragma unroll
     for (int q = 0; q < Q; ++q) f_o[(size_t)q * N + n] = v[q];
   }
   if (g_o) {
-    fetch_pop<T, S, RAW, false, false>(v, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
+    fetch_pop<T, S, RAW, false, false, false, true>(v, k, s.gin, s.phi_in, n, N, nb, c, eps, T(1));
 #pragma unroll
     for (int q = 0; q < Q; ++q) g_o[(size_t)q * N + n] = v[q];
   }
@@ -1576,16 +1590,22 @@ __global__ void __launch_bounds__(kBlock) k_measure(int nx, int ny, int nz, cons
 // component stride us), rho = phi rho_l + (1 - phi) rho_g, accumulated in
 // float64 per node in a fixed order (block partials, then the last block
 // sums them in block order).  Writes out3.
+// u in the state's layout: nh pairs (paired layout) or 0 (linear).
+struct NhOnly {
+  int nh;
+};
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_momentum(int N, const T* __restrict__ phi, const T* __restrict__ u,
-                                                    int us, double rho_l, double rho_g, double* partials,
+                                                    int us, int nh, double rho_l, double rho_g, double* partials,
                                                     unsigned* counter, double* out3) {
   double m[3] = {0.0, 0.0, 0.0};
+  const NhOnly lay{nh};
   for (int n = blockIdx.x * kBlock + threadIdx.x; n < N; n += gridDim.x * kBlock) {
     const double p = (double)phi[n];
     const double rho = p * rho_l + (1.0 - p) * rho_g;
+    const unsigned e = sidx(lay, n);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) m[d] += rho * (double)u[(size_t)d * us + n];
+    for (int d = 0; d < 3; ++d) m[d] += rho * (double)u[(size_t)d * us + e];
   }
   __shared__ double sw[kBlock / 32][3];
   __shared__ bool s_last;
@@ -1693,10 +1713,10 @@ cudaError_t launch_step(const Consts<T>& k, const State<T, S>& s, const Tiling& 
 // Launch with programmatic stream serialization (see pdl_wait).
 constexpr int kPdlOn = 1;  // 0: plain stream serialization
 template <typename... KArgs, typename... Args>
-static cudaError_t launch_pdl(void (*fn)(KArgs...), int blocks, cudaStream_t st, Args... args) {
+static cudaError_t launch_pdl_bs(void (*fn)(KArgs...), int blocks, int threads, cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)blocks);
-  cfg.blockDim = dim3(kBlock);
+  cfg.blockDim = dim3((unsigned)threads);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
@@ -1705,6 +1725,10 @@ static cudaError_t launch_pdl(void (*fn)(KArgs...), int blocks, cudaStream_t st,
   cfg.attrs = at;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, fn, args...);
+}
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*fn)(KArgs...), int blocks, cudaStream_t st, Args... args) {
+  return launch_pdl_bs(fn, blocks, kBlock, st, args...);
 }
 
 // Batched step kernels over a device case table; blocks: the grid (the
@@ -1729,6 +1753,38 @@ cudaError_t launch_update_batch(const void* cases, const unsigned short* b2c, in
   }
   if (omega1) return launch_pdl(k_update_batch<T, S, true>, blocks, st, c, b2c);
   return launch_pdl(k_update_batch<T, S, false>, blocks, st, c, b2c);
+}
+// The paired-layout step kernels over a device case table of paired grids.
+// (float compute only: float64 grids keep the linear layout)
+template <typename T, typename S>
+cudaError_t launch_phi_pair(const void* cases, const unsigned short* b2c, int blocks, cudaStream_t st) {
+  if constexpr (sizeof(T) == 8) {
+    return cudaErrorNotSupported;
+  } else {
+    if (blocks <= 0) return cudaSuccess;
+    return launch_pdl(k_phi_pair<T, S>, blocks, st, static_cast<const CaseDesc<T, S>*>(cases), b2c);
+  }
+}
+template <typename T, typename S>
+cudaError_t launch_update_pair(const void* cases, const unsigned short* b2c, int blocks, bool omega1,
+                               cudaStream_t st, bool gmu) {
+  if constexpr (sizeof(T) == 8) {
+    return cudaErrorNotSupported;
+  } else {
+    if (blocks <= 0) return cudaSuccess;
+    auto c = static_cast<const CaseDesc<T, S>*>(cases);
+    constexpr int bs = kPairUpdBlock;
+    if (gmu) {
+      if constexpr (sizeof(S) != 2) {
+        if (omega1) return launch_pdl_bs(k_update_pair<T, S, true, true>, blocks, bs, st, c, b2c);
+        return launch_pdl_bs(k_update_pair<T, S, false, true>, blocks, bs, st, c, b2c);
+      } else {
+        return cudaErrorNotSupported;
+      }
+    }
+    if (omega1) return launch_pdl_bs(k_update_pair<T, S, true, false>, blocks, bs, st, c, b2c);
+    return launch_pdl_bs(k_update_pair<T, S, false, false>, blocks, bs, st, c, b2c);
+  }
 }
 // k_mu and k_gradmu of one grid (plain stream order: they wait for the phi kernel, and the
 // next update kernel waits for it).
@@ -1803,17 +1859,17 @@ cudaError_t launch_measure(int nx, int ny, int nz, const T* phi, const uint8_t* 
   return cudaGetLastError();
 }
 template <typename T>
-cudaError_t launch_momentum(int N, const T* phi, const T* u, int us, double rho_l, double rho_g, double* partials,
-                            int max_blocks, unsigned* counter, double* out3, cudaStream_t st) {
+cudaError_t launch_momentum(int N, const T* phi, const T* u, int us, int nh, double rho_l, double rho_g,
+                            double* partials, int max_blocks, unsigned* counter, double* out3, cudaStream_t st) {
   int grid = (N + kBlock - 1) / kBlock;
   if (grid > max_blocks) grid = max_blocks;
-  k_momentum<T><<<grid, kBlock, 0, st>>>(N, phi, u, us, rho_l, rho_g, partials, counter, out3);
+  k_momentum<T><<<grid, kBlock, 0, st>>>(N, phi, u, us, nh, rho_l, rho_g, partials, counter, out3);
   return cudaGetLastError();
 }
-template cudaError_t launch_momentum<float>(int, const float*, const float*, int, double, double, double*, int,
+template cudaError_t launch_momentum<float>(int, const float*, const float*, int, int, double, double, double*, int,
                                             unsigned*, double*, cudaStream_t);
-template cudaError_t launch_momentum<double>(int, const double*, const double*, int, double, double, double*, int,
-                                             unsigned*, double*, cudaStream_t);
+template cudaError_t launch_momentum<double>(int, const double*, const double*, int, int, double, double, double*,
+                                             int, unsigned*, double*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Allocation-free spread diagnostics.  Some callers cannot allocate device
@@ -1908,6 +1964,9 @@ LBM_INSTANTIATE(float, __half)
   template cudaError_t launch_update_batch<T, S>(const void*, const unsigned short*, int, bool, cudaStream_t,    \
                                                  bool);                                                          \
   template cudaError_t launch_mu<T, S>(const Consts<T>&, const State<T, S>&, cudaStream_t);                     \
+  template cudaError_t launch_phi_pair<T, S>(const void*, const unsigned short*, int, cudaStream_t);            \
+  template cudaError_t launch_update_pair<T, S>(const void*, const unsigned short*, int, bool, cudaStream_t,     \
+                                                bool);                                                          \
   template size_t case_desc_bytes<T, S>();                                                                      \
   template void fill_case_desc<T, S>(void*, const Consts<T>&, const State<T, S>&, int, int, int, int);
 LBM_INSTANTIATE_BATCH(float, float)

@@ -1,11 +1,14 @@
 """Build liblbm_gb300.so in-tree for sm_103a.
 
-Five translation units compiled in parallel and linked with nvcc:
+Six translation units compiled in parallel and linked with nvcc:
   csrc/lbm_kernels.cu   device kernels (nvcc, sm_103a)
   csrc/lbm_kernels2d.cu device kernels of the 2-D D2Q9 form (nvcc, sm_103a)
   csrc/lbm_capi.cu      the C ABI of include/lbm_gb300.h (nvcc host code)
-  csrc/lbm_geometry.cpp host geometry precompute (g++, -ffp-contract=off so
-                        the float sequences match numpy bit for bit)
+  csrc/lbm_geometry.cu  device geometry precompute of a handle (explicitly
+                        rounded float operations; built without contraction)
+  csrc/lbm_geometry.cpp host geometry precompute of lbm_geometry_host (g++,
+                        -ffp-contract=off so the float sequences match numpy
+                        bit for bit)
   csrc/lbm_io.cpp       host output (the ASCII VTK writer)
 Output: lbm/_lib/liblbm_gb300.so next to this file.
 """
@@ -53,12 +56,13 @@ def build(force=False, verbose=False):
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC]
     jobs = []
-    for src in ("lbm_kernels.cu", "lbm_kernels2d.cu", "lbm_capi.cu"):
+    for src in ("lbm_kernels.cu", "lbm_kernels2d.cu", "lbm_geometry.cu", "lbm_capi.cu"):
         obj = os.path.join(obj_dir, src + ".o")
         # the 2-D kernels keep the reference's separate multiplies and adds
         # (no contraction into FMAs): their grids are small, and float32
-        # parity with the reference is closer without contraction
-        extra = ["-fmad=false"] if src == "lbm_kernels2d.cu" else []
+        # parity with the reference is closer without contraction; the
+        # geometry tables must be bit-exact
+        extra = ["-fmad=false"] if src in ("lbm_kernels2d.cu", "lbm_geometry.cu") else []
         jobs.append([nvcc, *common, *ARCH, "-lineinfo", *extra, "-Xcompiler", HOST_FLAGS, "-c",
                      os.path.join(CSRC, src), "-o", obj])
     for src in ("lbm_geometry.cpp", "lbm_io.cpp"):

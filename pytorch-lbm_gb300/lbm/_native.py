@@ -21,10 +21,11 @@ IFACE_ALLEN_CAHN, IFACE_CAHN_HILLIARD = 0, 1
 
 # every exported entry point declared in include/lbm_gb300.h
 EXPORTS = (
-    "lbm_create", "lbm_destroy", "lbm_set_geometry", "lbm_init_fields", "lbm_step", "lbm_step_profiled",
+    "lbm_create", "lbm_destroy", "lbm_set_geometry", "lbm_set_geometry_device", "lbm_init_fields", "lbm_step", "lbm_step_profiled",
     "lbm_get_fields", "lbm_get_populations", "lbm_get_geometry", "lbm_geometry_host",
     "lbm_get_scalars", "lbm_measure", "lbm_status", "lbm_last_error", "lbm_version",
-    "lbm_set_tile", "lbm_get_tile", "lbm_autotune", "lbm_measure_static", "lbm_footprint",
+    "lbm_set_tile", "lbm_get_tile", "lbm_set_layout", "lbm_get_layout", "lbm_autotune", "lbm_measure_static",
+    "lbm_footprint",
     "lbm_batch_create", "lbm_batch_step", "lbm_batch_size", "lbm_batch_autotune", "lbm_batch_destroy",
     "lbm_inject_droplet", "lbm_set_amplification", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
     "lbm_write_vtk", "lbm_reduce",
@@ -56,6 +57,7 @@ def _declare(L):
         "lbm_create": ([ctypes.POINTER(LbmParams), _i64, _i64, _i64, _i32, ctypes.POINTER(_vp)], _i32),
         "lbm_destroy": ([_vp], _i32),
         "lbm_set_geometry": ([_vp, _vp, _vp, _i32], _i32),
+        "lbm_set_geometry_device": ([_vp, _vp, _vp, _i32, _vp], _i32),
         "lbm_init_fields": ([_vp, _vp, _vp, _i32, _i32, _vp], _i32),
         "lbm_step": ([_vp, _i32, _vp], _i32),
         "lbm_step_profiled": ([_vp, _i32, _vp, ctypes.POINTER(ctypes.c_float)], _i32),
@@ -85,6 +87,8 @@ def _declare(L):
                         ctypes.POINTER(ctypes.c_float), _vp], _i32),
         "lbm_status": ([_vp, ctypes.POINTER(_u32)], _i32),
         "lbm_set_tile": ([_vp, _i32, _i32, _i32], _i32),
+        "lbm_set_layout": ([_vp, _i32], _i32),
+        "lbm_get_layout": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),
         "lbm_get_tile": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),
         "lbm_autotune": ([_vp, _i32, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)], _i32),
         "lbm_last_error": ([], ctypes.c_char_p),

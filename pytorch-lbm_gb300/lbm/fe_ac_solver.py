@@ -213,29 +213,37 @@ class AllenCahnSolver:
 
     # -- setup ----------------------------------------------------------------
     def set_solid(self, solid_mask, solid_fraction=None):
-        """lbm/fe_ac_solver.py:193-237 (geometry precompute in the native library)."""
-        solid = _host_array(solid_mask, np.bool_)
-        if solid.shape != self.shape:
-            raise ValueError(f"solid mask shape {solid.shape} != grid {self.shape}")
-        frac = None
+        """lbm/fe_ac_solver.py:193-237 (geometry precompute on the device).
+
+        The mask and the fraction (numpy arrays or tensors) are copied to the
+        device once; those copies become the ``solid`` and ``solid_fraction``
+        attributes and the inputs of the library's geometry kernels."""
+        def to_dev(x, dt):
+            t = x.detach() if torch.is_tensor(x) else torch.from_numpy(np.ascontiguousarray(np.asarray(x, dtype=dt)))
+            return t.to(device=self.device).contiguous()
+
+        solid_d = to_dev(solid_mask, np.bool_).to(torch.bool)
+        if tuple(solid_d.shape) != self.shape:
+            raise ValueError(f"solid mask shape {tuple(solid_d.shape)} != grid {self.shape}")
+        frac_d = None
         fdt = nat.LBM_DT_NONE
         if solid_fraction is not None:
-            fr = solid_fraction.detach().cpu().numpy() if torch.is_tensor(solid_fraction) else np.asarray(solid_fraction)
-            if fr.dtype == np.float32:
-                frac, fdt = np.ascontiguousarray(fr), nat.LBM_DT_F32
-            else:
-                frac, fdt = np.ascontiguousarray(fr, dtype=np.float64), nat.LBM_DT_F64
-            if frac.shape != self.shape:
-                raise ValueError(f"solid fraction shape {frac.shape} != grid {self.shape}")
-        s8 = solid.view(np.uint8)
-        nat.check(self._lib.lbm_set_geometry(self._h, s8.ctypes.data_as(ctypes.c_void_p),
-                                             frac.ctypes.data_as(ctypes.c_void_p) if frac is not None else None,
-                                             fdt), "lbm_set_geometry")
+            fr = solid_fraction if torch.is_tensor(solid_fraction) else np.asarray(solid_fraction)
+            is32 = fr.dtype in (np.float32, torch.float32)
+            frac_d = to_dev(fr, np.float32 if is32 else np.float64)
+            frac_d = frac_d.to(torch.float32 if is32 else torch.float64)
+            fdt = nat.LBM_DT_F32 if is32 else nat.LBM_DT_F64
+            if tuple(frac_d.shape) != self.shape:
+                raise ValueError(f"solid fraction shape {tuple(frac_d.shape)} != grid {self.shape}")
+        with torch.cuda.device(self.device):
+            nat.check(self._lib.lbm_set_geometry_device(self._h, nat.ptr(solid_d), nat.ptr(frac_d), fdt,
+                                                        nat.stream_ptr()), "lbm_set_geometry_device")
         self._geometry_set = True
-        self.solid = torch.from_numpy(solid.copy()).to(self.device)
-        self._solid_any = bool(solid.any())
-        if frac is not None:
-            self.solid_fraction = torch.tensor(frac, dtype=self.dtype, device=self.device)
+        self.solid = solid_d
+        if frac_d is not None:
+            self.solid_fraction = frac_d if frac_d.dtype == self.dtype else frac_d.to(self.dtype)
+        # the kernels read these device copies asynchronously: keep them until init_fields
+        self._geo_src = (solid_d, frac_d)
         self._tables = None  # the host tables of this geometry, fetched on first use
         cfg = self.config
         if cfg.theta_eq != 90.0 and cfg.kappa > 0:
@@ -305,6 +313,7 @@ class AllenCahnSolver:
                 nat.LBM_DT_F32 if npdt == np.float32 else nat.LBM_DT_F64, 0, stream), "lbm_init_fields")
             torch.cuda.current_stream().synchronize()
         self._keep = None
+        self._geo_src = None
         self._initialized = True
         self.step_count = 0
         self.t = 0.0
@@ -473,6 +482,20 @@ class AllenCahnSolver:
         t = (ctypes.c_int * 3)()
         nat.check(self._lib.lbm_get_tile(self._h, t), "lbm_get_tile")
         return tuple(t)
+
+    def set_layout(self, paired):
+        """Device storage layout (before ``init_fields``): linear (one element
+        per node, the default) or paired (nodes x and x + nx/2 in one word,
+        stepped a pair per thread; 3-D float32 / float16 grids with even nx).
+        The fields and populations read back are the same in either."""
+        nat.check(self._lib.lbm_set_layout(self._h, 1 if paired else 0), "lbm_set_layout")
+
+    @property
+    def paired(self):
+        """True when the state uses the paired storage layout."""
+        v = ctypes.c_int()
+        nat.check(self._lib.lbm_get_layout(self._h, ctypes.byref(v)), "lbm_get_layout")
+        return bool(v.value)
 
     # -- checkpoints and snapshots ---------------------------------------------
     def state_dict(self):
