@@ -418,6 +418,7 @@ def run_ours(args, rank, world, device):
                        "mode": args.mode,
                        "layout": "paired" if s.paired else "linear",
                        "tile": list(tile), "tuned_ms": tune_ms,
+                       "launch": dict(zip(("phi_nodes_per_thread", "update_block"), s.launch_shape())),
                        "l2": f"state (f, g: {4 * s.lattice.q * n * (2 if f16 else 4) / 1e6:.0f} MB) larger "
                              "than L2 (129 MB): no flush"},
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
@@ -466,9 +467,10 @@ def run_sweep(args, device):
     96^3 / 128x128x96 / 150x150x107 / 192x192x128, four substrates, R_d, theta,
     u_z drawn per case) advanced `--sweep-steps` steps each.  Timed: the
     batched half-precision form (one launch per kernel per step for all cases,
-    CUDA graph, autotuned phi kernel), the batched float32 form, and the plain
-    form (float32, one case at a time, each run to completion); device time
-    only, with the state resident.  Check: spread factor D/(2 R_d), aspect k and
+    CUDA graph, autotuned launch shape), the batched float32 form, both again
+    as one cooperative launch per step, and the plain form (float32, one case
+    at a time, each run to completion); device time only, with the state
+    resident.  Check: spread factor D/(2 R_d), aspect k and
     volume of the first `--sweep-check` cases against float64 runs."""
     import torch
     from lbm.batch import AllenCahnBatch
@@ -477,13 +479,16 @@ def run_sweep(args, device):
     cases = [sample_impact_case(args.seed + i, SWEEP_GRIDS, (n_steps, n_steps)) for i in range(args.sweep_cases)]
     updates = float(sum(c.nodes for c in cases)) * n_steps
 
-    def batched(dtype):
+    def batched(dtype, coop=False):
         t = time.perf_counter()
         solvers = [build_impact_case(c, dtype) for c in cases]
         setup = time.perf_counter() - t
         b = AllenCahnBatch(solvers)
+        if coop:
+            b.set_cooperative(True)
         b.run(1)
-        per, _ = b.autotune(reps=3)
+        b.autotune(reps=3)
+        per = b.launch_shape()
         secs = _events_time(lambda: b.run(n_steps - 1), device)
         meas = [s.measure() for s in solvers[:args.sweep_check]]
         b.close()
@@ -493,6 +498,9 @@ def run_sweep(args, device):
 
     m16, t16, set16, per16, meas16 = batched(torch.float16)
     m32b, t32b, _, per32, meas32 = batched(torch.float32)
+    # the same batches stepped by one cooperative launch per step (A/B)
+    c16, ct16, _, cper16, _ = batched(torch.float16, coop=True)
+    c32, ct32, _, cper32, _ = batched(torch.float32, coop=True)
     plain = 0.0
     for c in cases:
         s = build_impact_case(c, torch.float32)
@@ -519,8 +527,10 @@ def run_sweep(args, device):
                                    "R_d~U[15,30], theta~U[90,162], u_z~U[-0.08,-0.02], seeds "
                                    f"{args.seed}..{args.seed + len(cases) - 1}",
                        "node_updates": updates},
-            "batched_f16": {"mlups": m16, "seconds": t16, "setup_s": set16, "phi_nodes_per_thread": per16},
-            "batched_f32": {"mlups": m32b, "seconds": t32b, "phi_nodes_per_thread": per32},
+            "batched_f16": {"mlups": m16, "seconds": t16, "setup_s": set16, "launch_shape": per16},
+            "batched_f32": {"mlups": m32b, "seconds": t32b, "launch_shape": per32},
+            "batched_f16_single_launch": {"mlups": c16, "seconds": ct16, "launch_shape": cper16},
+            "batched_f32_single_launch": {"mlups": c32, "seconds": ct32, "launch_shape": cper32},
             "plain_f32": {"mlups": m32p, "seconds": plain, "what": "one case at a time, each to completion"},
             "speedup_f16_batched_vs_plain_f32": m16 / m32p,
             "fp64_check": check}
@@ -531,12 +541,14 @@ def run_precision(args, device):
     droplet R = 45 at height 180, u_z = -0.06, theta = 150): the same case in
     half-precision population storage, float32 and float64 for
     `--precision-steps` steps each; device time per form; spread factor
-    beta = max(Dx, Dy) / (2 R), aspect k, contact angle and sum(phi) drift of
-    each form every `--precision-every` steps, and the half and float32 forms'
-    errors against the float64 run (the oracle at this size)."""
+    beta = max(Dx, Dy) / (2 R), aspect k, contact angles (the reference's
+    layer scan, and the angle against the local wall normal that a curved
+    substrate needs) and sum(phi) drift of each form every
+    `--precision-every` steps, and the half and float32 forms' errors against
+    the float64 run (the oracle at this size)."""
     import torch
     from lbm.fe_ac_solver import AllenCahnSolver
-    from lbm.fe_measure import measure_contact_angle
+    from lbm.fe_measure import measure_contact_angle, measure_contact_angle_wall
     cfg, solid, frac, C, u = make_case("convex384")
     cfg.device = str(device)
     w = WORKLOADS["convex384"]
@@ -556,9 +568,12 @@ def run_precision(args, device):
             secs += _events_time(lambda: s.run(k), device)
             done += k
             m = s.measure()
-            ca = measure_contact_angle(s.phi, s.solid)
+            phi = s.phi
+            ca = measure_contact_angle(phi, s.solid)
+            caw = measure_contact_angle_wall(phi, s.solid, s.wetting.wall_normal, s.wetting.is_boundary)
             hist.append({"step": done, "beta": max(m["Dx"], m["Dy"]) / (2.0 * w["radius"]), "k": m["k"],
-                         "contact_angle": ca, "mass_drift": (m["volume"] - m0) / m0, "nan": m["has_nan"]})
+                         "contact_angle": ca, "contact_angle_wall": caw, "mass_drift": (m["volume"] - m0) / m0,
+                         "nan": m["has_nan"]})
         forms[name] = {"ms_per_step": secs * 1e3 / K, "mlups": n * K / secs / 1e6, "setup_s": setup,
                        "history": hist}
         s.close()
@@ -571,6 +586,10 @@ def run_precision(args, device):
             "beta_rel_err": abs(last["beta"] - ref["beta"]) / ref["beta"] if ref["beta"] else None,
             "k_abs_err": abs(last["k"] - ref["k"]),
             "contact_angle_abs_err_deg": abs(last["contact_angle"] - ref["contact_angle"]),
+            "contact_angle_wall_abs_err_deg": abs(last["contact_angle_wall"] - ref["contact_angle_wall"]),
+            "max_contact_angle_wall_err_over_run_deg": max(abs(a["contact_angle_wall"] - b["contact_angle_wall"])
+                                                           for a, b in zip(forms[name]["history"],
+                                                                           forms["f64"]["history"])),
             "mass_drift_diff": last["mass_drift"] - ref["mass_drift"],
             "max_beta_rel_err_over_run": max(abs(a["beta"] - b["beta"]) / b["beta"] if b["beta"] else 0.0
                                              for a, b in zip(forms[name]["history"], forms["f64"]["history"]))}

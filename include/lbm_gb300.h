@@ -185,12 +185,26 @@ int lbm_get_tile(LbmHandle* h, int* txyz3);
 int lbm_set_layout(LbmHandle* h, int paired);
 int lbm_get_layout(LbmHandle* h, int* paired);
 
-/* Step autotuner: times `reps` launches of the next step for the two-kernel
- * step and for each candidate tile shape of the fused kernel on the handle's
- * current state (which it leaves unchanged) and keeps the fastest.  Synchronises `stream`; allocates a
- * temporary copy of u.  Outputs (may be NULL): the chosen extents and its
- * time per launch in ms.  No reference counterpart. */
+/* Step autotuner: times `reps` launches of the next step on the handle's
+ * current state (which it leaves unchanged) for each candidate and keeps the
+ * fastest: the two-kernel step with each phi-kernel work size (4, 8, 12, 16,
+ * 24 or 32 nodes per thread) and each update-kernel block (128 or 256
+ * threads; 256 only in the gradient-of-mu modes, and the paired layout's
+ * update kernel has its fixed block), and each candidate tile shape of the
+ * fused kernel.  Synchronises `stream`; allocates a temporary copy of u.
+ * Outputs (may be NULL): the chosen extents and its time per launch in ms;
+ * lbm_get_launch gives the chosen work size and block.  No reference
+ * counterpart. */
 int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* best_ms);
+
+/* Launch shape of the two-kernel step: the phi kernel's nodes per thread
+ * (1..64) and the linear-layout update kernel's threads per block (128 or
+ * 256; 256 in the gradient-of-mu modes).  Results do not depend on it; speed
+ * does.  lbm_get_launch reports the shape in use (either output may be NULL;
+ * the paired layout's update block is fixed at 128).  No reference
+ * counterpart. */
+int lbm_set_launch(LbmHandle* h, int phi_nodes_per_thread, int update_block);
+int lbm_get_launch(LbmHandle* h, int* phi_nodes_per_thread, int* update_block);
 
 /* Write the fields the reference exposes after the last step (or after
  * init) into caller device buffers of the handle's compute type (float for
@@ -364,12 +378,27 @@ int lbm_batch_step(LbmBatch* b, int nsteps, void* stream);
 /* Number of cases. */
 int lbm_batch_size(LbmBatch* b, int* ncases);
 
-/* Autotuner of the batched phi kernel's nodes per thread (its block count per
- * case): times `reps` batched steps that re-read the current state for each
- * candidate and keeps the fastest; the state is left unchanged.  Every case
- * must have taken a step.  Synchronises `stream`; allocates temporary copies
- * of u.  Outputs (may be NULL): the choice and its time per step in ms. */
+/* Autotuner of the batched step's launch shape: the phi kernel's nodes per
+ * thread (1, 2, 4, 8, 12, 16, 24 or 32: its block count per case) and the
+ * update kernel's threads per block (128 or 256).  Times `reps` batched
+ * steps that re-read the current state for each candidate pair and keeps the
+ * fastest; the state is left unchanged.  Every case must have taken a step.
+ * Synchronises `stream`; allocates temporary copies of u.  Outputs (may be
+ * NULL): the chosen nodes per thread and the time per step in ms;
+ * lbm_batch_get_launch gives both choices. */
 int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread, float* best_ms);
+
+/* The batch's launch shape: phi-kernel nodes per thread and update-kernel
+ * threads per block (either output may be NULL). */
+int lbm_batch_get_launch(LbmBatch* b, int* phi_nodes_per_thread, int* update_block);
+
+/* on = 1: every batched step is ONE cooperative launch (a grid of resident
+ * blocks runs the phi work of every case, a grid-wide barrier, then the update
+ * work of every case) instead of the two launches of the phi and update
+ * kernels; on = 0 (the default): the two launches.  Same results bit for bit.
+ * Linear-layout cases only (LBM_E_UNSUPPORTED otherwise); the update work
+ * then runs 256-thread blocks.  No reference counterpart. */
+int lbm_batch_set_cooperative(LbmBatch* b, int on);
 
 /* Free the batch (not its handles). */
 int lbm_batch_destroy(LbmBatch* b);

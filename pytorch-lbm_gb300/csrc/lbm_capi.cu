@@ -44,13 +44,15 @@ cudaError_t launch_measure_static(int, int, int, const T*, const uint8_t*, doubl
 template <typename T, typename S>
 cudaError_t launch_phi_batch(const void*, const unsigned short*, int, cudaStream_t);
 template <typename T, typename S>
-cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, cudaStream_t, bool = false);
+cudaError_t launch_update_batch(const void*, const unsigned short*, int, bool, cudaStream_t, bool, int);
 template <typename T, typename S>
 cudaError_t launch_mu(const Consts<T>&, const State<T, S>&, cudaStream_t);
 template <typename T, typename S>
 cudaError_t launch_phi_pair(const void*, const unsigned short*, int, cudaStream_t);
 template <typename T, typename S>
 cudaError_t launch_update_pair(const void*, const unsigned short*, int, bool, cudaStream_t, bool);
+template <typename T, typename S>
+cudaError_t launch_batch_coop(const void*, const unsigned short*, int, int, int, cudaStream_t);
 
 // the 2-D (nz == 1, D2Q9) form (lbm_kernels2d.cu)
 template <typename T, typename Src>
@@ -151,6 +153,7 @@ struct LbmHandle {
   bool desc_ok = false;
   int desc_cur0 = 0;        // cur when the descriptors were filled (parity 0)
   int phi_per_thread = 16;  // nodes per thread of the phi kernel
+  int upd_block = kBlock;   // threads per block of the (linear-layout) update kernel: 128 or 256
 };
 
 namespace {
@@ -439,8 +442,10 @@ int phi_blocks_of(const LbmHandle* h, int per_thread) {
   const long long per = (long long)kBlock * (h->paired ? std::max(1, per_thread / 2) : per_thread);
   return (int)std::max<long long>(1, (units_of(h) + per - 1) / per);
 }
-int upd_blocks_of(const LbmHandle* h) {
-  const int64_t bs = h->paired ? kPairUpdBlock : kBlock;
+// upd_block: threads per block of the linear-layout update kernel (the
+// paired update kernel always runs kPairUpdBlock).
+int upd_blocks_of(const LbmHandle* h, int upd_block) {
+  const int64_t bs = h->paired ? kPairUpdBlock : upd_block;
   return (int)((units_of(h) + bs - 1) / bs);
 }
 
@@ -452,9 +457,9 @@ cudaError_t launch_phi_kernel(bool paired, const void* cases, const unsigned sho
 }
 template <typename T, typename S>
 cudaError_t launch_update_kernel(bool paired, const void* cases, const unsigned short* b2c, int blocks, bool omega1,
-                                 cudaStream_t st, bool gmu) {
+                                 cudaStream_t st, bool gmu, int upd_block) {
   return paired ? launch_update_pair<T, S>(cases, b2c, blocks, omega1, st, gmu)
-                : launch_update_batch<T, S>(cases, b2c, blocks, omega1, st, gmu);
+                : launch_update_batch<T, S>(cases, b2c, blocks, omega1, st, gmu, upd_block);
 }
 
 // The handle's one-case descriptor table for the batched kernels: [0] the
@@ -470,7 +475,7 @@ int fill_desc(LbmHandle* h, cudaStream_t st) {
     s.c_prev = h->c_last ^ par;
     s.c_cur = h->c_last ^ par ^ 1;
     fill_case_desc<T, S>(buf.data() + par * db, consts_of<T>(*h), s, 0, phi_blocks_of(h, h->phi_per_thread), 0,
-                         upd_blocks_of(h));
+                         upd_blocks_of(h, h->upd_block));
   }
   // earlier steps on `st` may still read the old table
   CUDA_TRY(cudaStreamSynchronize(st));
@@ -501,7 +506,8 @@ int launch_next(LbmHandle* h, const Tiling& t, cudaStream_t st, cudaEvent_t mid)
       State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
       CUDA_TRY((launch_mu<T, S>(consts_of<T>(*h), s, st)));
     }
-    CUDA_TRY((launch_update_kernel<T, S>(h->paired, d, nullptr, upd_blocks_of(h), omega1_of(h), st, gmu)));
+    CUDA_TRY((launch_update_kernel<T, S>(h->paired, d, nullptr, upd_blocks_of(h, h->upd_block), omega1_of(h), st,
+                                         gmu, h->upd_block)));
     return LBM_OK;
   }
   State<T, S> s = make_state<T, S>(*h, h->cur, h->pc);
@@ -942,33 +948,43 @@ int lbm_autotune(LbmHandle* h, int reps, void* stream, int* best_txyz3, float* b
     }
   }
   Tiling best = h->tiling;
-  int best_per = h->phi_per_thread;
+  int best_per = h->phi_per_thread, best_bs = h->upd_block;
   float best_t = 1e30f;
   int rc = LBM_OK;
   for (const Tiling& t : cands) {
-    // the two-kernel step: also its phi kernel's nodes per thread
+    // the two-kernel step: also its phi kernel's nodes per thread and the
+    // update kernel's threads per block (256 only for the gradient-of-mu modes
+    // and the paired layout, whose update kernel has a fixed block)
     const std::vector<int> pers =
         t.tx == 0 ? std::vector<int>{4, 8, 12, 16, 24, 32} : std::vector<int>{h->phi_per_thread};
-    for (int per : pers) {
-      if (per != h->phi_per_thread) {
-        h->phi_per_thread = per;
-        h->desc_ok = false;
+    const std::vector<int> bss =
+        (t.tx == 0 && !h->mu && !h->paired) ? std::vector<int>{128, kBlock} : std::vector<int>{h->upd_block};
+    for (int bs : bss) {
+      for (int per : pers) {
+        if (per != h->phi_per_thread || bs != h->upd_block) {
+          h->phi_per_thread = per;
+          h->upd_block = bs;
+          h->desc_ok = false;
+        }
+        float ms = 0.f;
+        rc = with_types(h->prec, [&](auto tag) {
+          return time_tiling<typename decltype(tag)::T, typename decltype(tag)::S>(h, t, reps, st, e0, e1, &ms);
+        });
+        if (rc != LBM_OK) break;
+        if (ms < best_t) {
+          best_t = ms;
+          best = t;
+          best_per = per;
+          best_bs = bs;
+        }
       }
-      float ms = 0.f;
-      rc = with_types(h->prec, [&](auto tag) {
-        return time_tiling<typename decltype(tag)::T, typename decltype(tag)::S>(h, t, reps, st, e0, e1, &ms);
-      });
       if (rc != LBM_OK) break;
-      if (ms < best_t) {
-        best_t = ms;
-        best = t;
-        best_per = per;
-      }
     }
     if (rc != LBM_OK) break;
   }
-  if (h->phi_per_thread != best_per) {
+  if (h->phi_per_thread != best_per || h->upd_block != best_bs) {
     h->phi_per_thread = best_per;
+    h->upd_block = best_bs;
     h->desc_ok = false;
   }
   cudaMemcpyAsync(h->u, u_save, ub, cudaMemcpyDeviceToDevice, st);
@@ -1004,6 +1020,27 @@ int lbm_set_layout(LbmHandle* h, int paired) {
 int lbm_get_layout(LbmHandle* h, int* paired) {
   if (!h || !paired) return fail(LBM_E_ARG, "lbm_get_layout: null argument");
   *paired = h->paired ? 1 : 0;
+  return LBM_OK;
+}
+
+int lbm_set_launch(LbmHandle* h, int phi_nodes_per_thread, int update_block) {
+  if (!h) return fail(LBM_E_ARG, "lbm_set_launch: null handle");
+  if (phi_nodes_per_thread < 1 || phi_nodes_per_thread > 64)
+    return fail(LBM_E_ARG, "lbm_set_launch: phi_nodes_per_thread must be in [1, 64]");
+  if (update_block != 128 && update_block != kBlock)
+    return fail(LBM_E_ARG, "lbm_set_launch: update_block must be 128 or 256");
+  if (update_block != kBlock && h->mu)
+    return fail(LBM_E_UNSUPPORTED, "lbm_set_launch: the gradient-of-mu modes run 256-thread update blocks");
+  h->phi_per_thread = phi_nodes_per_thread;
+  h->upd_block = update_block;
+  h->desc_ok = false;
+  return LBM_OK;
+}
+
+int lbm_get_launch(LbmHandle* h, int* phi_nodes_per_thread, int* update_block) {
+  if (!h) return fail(LBM_E_ARG, "lbm_get_launch: null handle");
+  if (phi_nodes_per_thread) *phi_nodes_per_thread = h->phi_per_thread;
+  if (update_block) *update_block = h->paired ? kPairUpdBlock : h->upd_block;
   return LBM_OK;
 }
 
@@ -1444,6 +1481,8 @@ struct LbmBatch {
   // with omega_f == 1, 1 linear other, 2 paired layout with omega_f == 1, 3 paired other
   int gstart[5] = {0, 0, 0, 0, 0};
   int phi_per_thread = 16;  // nodes per phi-kernel thread (half as many pairs in the paired layout)
+  int upd_block = kBlock;   // threads per block of the linear-layout update kernel
+  bool coop = false;        // one cooperative launch per step (k_batch_coop) instead of two launches
   size_t desc = 0;          // bytes of one case descriptor
   void* table[2] = {nullptr, nullptr};  // device descriptors: [0] this step, [1] the next
   unsigned char* staging = nullptr;     // pinned host copy of both tables
@@ -1470,7 +1509,7 @@ int batch_layout(LbmBatch* b) {
   long long pb[2] = {0, 0}, ub[4] = {0, 0, 0, 0};
   for (int i = 0; i < n; ++i) {
     pb[b->h[i]->paired ? 1 : 0] += phi_blocks_of(b->h[i], b->phi_per_thread);
-    ub[launch_group(b->h[i])] += upd_blocks_of(b->h[i]);
+    ub[launch_group(b->h[i])] += upd_blocks_of(b->h[i], b->upd_block);
   }
   const long long tot = pb[0] + pb[1] + ub[0] + ub[1] + ub[2] + ub[3];
   if (tot > 0x7fffffff) return fail(LBM_E_ARG, "lbm_batch: grids too large");
@@ -1486,7 +1525,7 @@ int batch_layout(LbmBatch* b) {
     size_t& a = at[b->h[i]->paired ? 1 : 0];
     for (int k = phi_blocks_of(b->h[i], b->phi_per_thread); k > 0; --k) t[a++] = (unsigned short)i;
     size_t& c = at[2 + launch_group(b->h[i])];
-    for (int k = upd_blocks_of(b->h[i]); k > 0; --k) t[c++] = (unsigned short)i;
+    for (int k = upd_blocks_of(b->h[i], b->upd_block); k > 0; --k) t[c++] = (unsigned short)i;
   }
   CUDA_TRY(cudaMalloc(&b->b2c, t.size() * sizeof(unsigned short)));
   CUDA_TRY(cudaMemcpy(b->b2c, t.data(), t.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
@@ -1500,7 +1539,8 @@ void batch_fill_t(LbmBatch* b) {
   int pb[2] = {0, 0}, ub[4] = {0, 0, 0, 0};
   for (int i = 0; i < n; ++i) {
     LbmHandle* h = b->h[i];
-    const int phin = phi_blocks_of(h, b->phi_per_thread), updn = upd_blocks_of(h), g = launch_group(h);
+    const int phin = phi_blocks_of(h, b->phi_per_thread), updn = upd_blocks_of(h, b->upd_block),
+              g = launch_group(h);
     int& pbl = pb[h->paired ? 1 : 0];
     for (int par = 0; par < 2; ++par) {
       State<T, S> s = make_state<T, S>(*h, h->cur ^ par, h->pc ^ par);
@@ -1533,6 +1573,8 @@ int batch_fill(LbmBatch* b, cudaStream_t st) {
 // each group (layout x omega_f == 1 or not).  Empty launches are skipped.
 template <typename T, typename S>
 cudaError_t batch_launch_t(LbmBatch* b, int par, cudaStream_t st) {
+  if (b->coop)
+    return launch_batch_coop<T, S>(b->table[par], b->b2c, b->phi_blocks[0], b->upd_blocks[0], b->upd_blocks[1], st);
   const unsigned short* t = b->b2c;
   cudaError_t e = cudaSuccess;
   for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
@@ -1540,7 +1582,8 @@ cudaError_t batch_launch_t(LbmBatch* b, int par, cudaStream_t st) {
     t += b->phi_blocks[j];
   }
   for (int g = 0; g < 4 && e == cudaSuccess; ++g) {
-    e = launch_update_kernel<T, S>(g >= 2, b->table[par], t, b->upd_blocks[g], (g & 1) == 0, st, false);
+    e = launch_update_kernel<T, S>(g >= 2, b->table[par], t, b->upd_blocks[g], (g & 1) == 0, st, false,
+                                   b->upd_block);
     t += b->upd_blocks[g];
   }
   return e;
@@ -1685,6 +1728,26 @@ int lbm_batch_step(LbmBatch* b, int nsteps, void* stream) {
   return LBM_OK;
 }
 
+int lbm_batch_set_cooperative(LbmBatch* b, int on) {
+  if (!b) return fail(LBM_E_ARG, "lbm_batch_set_cooperative: null batch");
+  if (on != 0 && on != 1) return fail(LBM_E_ARG, "lbm_batch_set_cooperative: on must be 0 or 1");
+  if (on) {
+    for (LbmHandle* h : b->h)
+      if (h->paired)
+        return fail(LBM_E_UNSUPPORTED, "lbm_batch_set_cooperative: the single-launch step serves linear-layout cases");
+  }
+  b->coop = on != 0;
+  if (b->coop) b->upd_block = kBlock;
+  return batch_layout(b);
+}
+
+int lbm_batch_get_launch(LbmBatch* b, int* phi_nodes_per_thread, int* update_block) {
+  if (!b) return fail(LBM_E_ARG, "lbm_batch_get_launch: null batch");
+  if (phi_nodes_per_thread) *phi_nodes_per_thread = b->phi_per_thread;
+  if (update_block) *update_block = b->upd_block;
+  return LBM_OK;
+}
+
 int lbm_batch_size(LbmBatch* b, int* ncases) {
   if (!b || !ncases) return fail(LBM_E_ARG, "lbm_batch_size: null argument");
   *ncases = (int)b->h.size();
@@ -1708,10 +1771,13 @@ int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0));
   CUDA_TRY(cudaEventCreate(&e1));
-  int best = b->phi_per_thread, rc = LBM_OK;
+  int best = b->phi_per_thread, best_bs = b->upd_block, rc = LBM_OK;
   float best_t = 1e30f;
+  for (int bs : {128, kBlock})
   for (int per : {1, 2, 4, 8, 12, 16, 24, 32}) {
+    if (b->coop && bs != kBlock) continue;  // the cooperative step runs 256-thread update blocks
     b->phi_per_thread = per;
+    b->upd_block = bs;
     rc = batch_layout(b);
     if (rc == LBM_OK) rc = batch_fill(b, st);
     if (rc != LBM_OK) break;
@@ -1729,6 +1795,7 @@ int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread
     if (ms < best_t) {
       best_t = ms;
       best = per;
+      best_bs = bs;
     }
   }
   for (size_t i = 0; i < b->h.size(); ++i) {
@@ -1741,6 +1808,7 @@ int lbm_batch_autotune(LbmBatch* b, int reps, void* stream, int* best_per_thread
   cudaEventDestroy(e1);
   if (rc != LBM_OK) return rc;
   b->phi_per_thread = best;
+  b->upd_block = best_bs;
   rc = batch_layout(b);
   if (rc != LBM_OK) return rc;
   if (best_per_thread) *best_per_thread = best;

@@ -29,9 +29,11 @@
 // matters for parity; the isotropic gradient is accumulated without FMA
 // contraction.  (Measured and dropped for k_phi: runs of four consecutive
 // nodes per thread -- 43 -> 58 us, the per-thread runs break coalescing.)
+#include <cooperative_groups.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <type_traits>
@@ -1216,15 +1218,61 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 8 ? 3 : 4) k_phi_batch(co
   phi_finish(d.s, part, b, nb);
 }
 
-template <typename T, typename S, bool OMEGA1, bool GMU = false>
-__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S, GMU>::blocks) k_update_batch(
+// BS threads per block (the autotuners choose 128 or 256), compiled for the
+// same registers per thread at either size.
+template <typename T, typename S, bool OMEGA1, bool GMU = false, int BS = kBlock>
+__global__ void __launch_bounds__(BS, UpdateOccupancy<T, S, GMU>::blocks * kBlock / BS) k_update_batch(
     const CaseDesc<T, S>* __restrict__ cases, const unsigned short* __restrict__ blk2case) {
   __shared__ CaseDesc<T, S> d;
   load_desc(d, cases + (blk2case ? blk2case[blockIdx.x] : 0));
   pdl_trigger();
   pdl_wait();  // phi of the phi kernel (mu of k_mu with GMU)
-  const int n = (blockIdx.x - d.upd_blk0) * kBlock + threadIdx.x;
+  const int n = (blockIdx.x - d.upd_blk0) * BS + threadIdx.x;
   if (n < d.k.N) update_one<T, S, false, false, OMEGA1, GMU>(d.k, d.s, n, Pol::make());
+}
+
+// ---------------------------------------------------------------------------
+// The batched step as ONE cooperative launch: a grid of resident blocks runs
+// the phi kernel's virtual blocks (the block -> case table's phi part), a
+// grid-wide barrier (cooperative groups: every block of a cooperative launch
+// is resident, so the barrier ends), then the update kernel's virtual blocks.
+// Each virtual block does exactly what the block of the same index does in
+// k_phi_batch / k_update_batch (same descriptor, same nodes, same arithmetic,
+// the same last-block reduction per case), so the results are those of the
+// two-launch step bit for bit.  Linear-layout cases only.
+// ---------------------------------------------------------------------------
+template <typename T, typename S>
+__global__ void __launch_bounds__(kBlock, UpdateOccupancy<T, S>::blocks) k_batch_coop(
+    const CaseDesc<T, S>* __restrict__ cases, const unsigned short* __restrict__ b2c, int phi_blocks,
+    int upd_blocks_om1, int upd_blocks_other) {
+  __shared__ CaseDesc<T, S> d;
+  const Pol pol = Pol::make();
+  for (int vb = blockIdx.x; vb < phi_blocks; vb += gridDim.x) {
+    __syncthreads();  // the previous virtual block is done with d
+    load_desc(d, cases + b2c[vb]);
+    const int b = vb - d.phi_blk0, nb = d.phi_nblk;
+    TileSum<T> part;
+    const int N = d.k.N, stride = nb * kBlock;
+    int n = b * kBlock + threadIdx.x;
+    uint8_t c = n < N ? d.s.cls[n] : 0;
+    for (; n < N; n += stride) {
+      const uint8_t c_next = n + stride < N ? d.s.cls[n + stride] : 0;
+      phi_node<T, S, false>(d.k, d.s, n, c, pol, part);
+      c = c_next;
+    }
+    phi_finish(d.s, part, b, nb);
+  }
+  cooperative_groups::this_grid().sync();
+  const int upd_blocks = upd_blocks_om1 + upd_blocks_other;
+  for (int vb = blockIdx.x; vb < upd_blocks; vb += gridDim.x) {
+    __syncthreads();
+    load_desc(d, cases + b2c[phi_blocks + vb]);
+    const int n = (vb - (vb < upd_blocks_om1 ? 0 : upd_blocks_om1) - d.upd_blk0) * kBlock + threadIdx.x;
+    if (n < d.k.N) {
+      if (vb < upd_blocks_om1) update_one<T, S, false, false, true, false>(d.k, d.s, n, pol);
+      else update_one<T, S, false, false, false, false>(d.k, d.s, n, pol);
+    }
+  }
 }
 
 }  // namespace lbm
@@ -1738,19 +1786,27 @@ cudaError_t launch_phi_batch(const void* cases, const unsigned short* b2c, int b
   if (blocks <= 0) return cudaSuccess;
   return launch_pdl(k_phi_batch<T, S>, blocks, st, static_cast<const CaseDesc<T, S>*>(cases), b2c);
 }
+// bs: threads per block of the update kernel, 256 or (without the
+// gradient-of-mu modes) 128.
 template <typename T, typename S>
 cudaError_t launch_update_batch(const void* cases, const unsigned short* b2c, int blocks, bool omega1,
-                                cudaStream_t st, bool gmu) {
+                                cudaStream_t st, bool gmu, int bs) {
   if (blocks <= 0) return cudaSuccess;
   auto c = static_cast<const CaseDesc<T, S>*>(cases);
   if (gmu) {
     if constexpr (sizeof(S) != 2) {
+      if (bs != kBlock) return cudaErrorInvalidValue;
       if (omega1) return launch_pdl(k_update_batch<T, S, true, true>, blocks, st, c, b2c);
       return launch_pdl(k_update_batch<T, S, false, true>, blocks, st, c, b2c);
     } else {
       return cudaErrorNotSupported;
     }
   }
+  if (bs == 128) {
+    if (omega1) return launch_pdl_bs(k_update_batch<T, S, true, false, 128>, blocks, 128, st, c, b2c);
+    return launch_pdl_bs(k_update_batch<T, S, false, false, 128>, blocks, 128, st, c, b2c);
+  }
+  if (bs != kBlock) return cudaErrorInvalidValue;
   if (omega1) return launch_pdl(k_update_batch<T, S, true>, blocks, st, c, b2c);
   return launch_pdl(k_update_batch<T, S, false>, blocks, st, c, b2c);
 }
@@ -1786,6 +1842,46 @@ cudaError_t launch_update_pair(const void* cases, const unsigned short* b2c, int
     return launch_pdl_bs(k_update_pair<T, S, false, false>, blocks, bs, st, c, b2c);
   }
 }
+// The cooperative single-launch batched step (k_batch_coop) over a table
+// whose update blocks run 256 threads; grid: resident blocks of the kernel.
+template <typename T, typename S>
+cudaError_t launch_batch_coop(const void* cases, const unsigned short* b2c, int phi_blocks, int upd_om1,
+                              int upd_other, cudaStream_t st) {
+  static std::mutex mu;
+  static int cached_dev = -1, cached = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int grid;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (cached_dev != dev) {
+      int nsm = 0, b = 0;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_coop<T, S>, kBlock, 0);
+      if (e != cudaSuccess) return e;
+      cached = nsm * b;
+      cached_dev = dev;
+    }
+    grid = cached;
+  }
+  const int work = std::max(phi_blocks, upd_om1 + upd_other);
+  if (work <= 0) return cudaSuccess;
+  if (grid > work) grid = work;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_batch_coop<T, S>, static_cast<const CaseDesc<T, S>*>(cases), b2c, phi_blocks,
+                            upd_om1, upd_other);
+}
+
 // k_mu and k_gradmu of one grid (plain stream order: they wait for the phi kernel, and the
 // next update kernel waits for it).
 template <typename T, typename S>
@@ -1962,9 +2058,10 @@ LBM_INSTANTIATE(float, __half)
 #define LBM_INSTANTIATE_BATCH(T, S)                                                                             \
   template cudaError_t launch_phi_batch<T, S>(const void*, const unsigned short*, int, cudaStream_t);           \
   template cudaError_t launch_update_batch<T, S>(const void*, const unsigned short*, int, bool, cudaStream_t,    \
-                                                 bool);                                                          \
+                                                 bool, int);                                                     \
   template cudaError_t launch_mu<T, S>(const Consts<T>&, const State<T, S>&, cudaStream_t);                     \
   template cudaError_t launch_phi_pair<T, S>(const void*, const unsigned short*, int, cudaStream_t);            \
+  template cudaError_t launch_batch_coop<T, S>(const void*, const unsigned short*, int, int, int, cudaStream_t);  \
   template cudaError_t launch_update_pair<T, S>(const void*, const unsigned short*, int, bool, cudaStream_t,     \
                                                 bool);                                                          \
   template size_t case_desc_bytes<T, S>();                                                                      \

@@ -27,6 +27,7 @@ EXPORTS = (
     "lbm_set_tile", "lbm_get_tile", "lbm_set_layout", "lbm_get_layout", "lbm_autotune", "lbm_measure_static",
     "lbm_footprint",
     "lbm_batch_create", "lbm_batch_step", "lbm_batch_size", "lbm_batch_autotune", "lbm_batch_destroy",
+    "lbm_set_launch", "lbm_get_launch", "lbm_batch_get_launch", "lbm_batch_set_cooperative",
     "lbm_inject_droplet", "lbm_set_amplification", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
     "lbm_write_vtk", "lbm_reduce",
 )
@@ -76,6 +77,10 @@ def _declare(L):
         "lbm_batch_size": ([_vp, ctypes.POINTER(ctypes.c_int)], _i32),
         "lbm_batch_autotune": ([_vp, _i32, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)], _i32),
         "lbm_batch_destroy": ([_vp], _i32),
+        "lbm_set_launch": ([_vp, _i32, _i32], _i32),
+        "lbm_get_launch": ([_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], _i32),
+        "lbm_batch_get_launch": ([_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], _i32),
+        "lbm_batch_set_cooperative": ([_vp, _i32], _i32),
         "lbm_inject_droplet": ([_vp, ctypes.POINTER(_dbl), _dbl, _dbl, ctypes.POINTER(_dbl), ctypes.POINTER(_i64),
                                 _vp], _i32),
         "lbm_set_amplification": ([_vp, _vp, _i32], _i32),

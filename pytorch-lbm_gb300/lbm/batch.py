@@ -53,13 +53,26 @@ class AllenCahnBatch:
         self.run(1)
 
     def autotune(self, reps=5, stream=None):
-        """Nodes per thread of the batched phi kernel: the fastest candidate on
-        the current state (left unchanged).  Returns (choice, ms per step)."""
+        """Launch shape of the batched step (the phi kernel's nodes per thread
+        and the update kernel's threads per block): the fastest candidate on
+        the current state (left unchanged).  Returns (nodes per thread, ms per
+        step); ``launch_shape()`` gives both choices."""
         best = ctypes.c_int()
         ms = ctypes.c_float()
         nat.check(self._lib.lbm_batch_autotune(self._h, int(reps), nat.stream_ptr(stream), ctypes.byref(best),
                                                ctypes.byref(ms)), "lbm_batch_autotune")
         return int(best.value), float(ms.value)
+
+    def set_cooperative(self, on=True):
+        """One cooperative launch per batched step (phi work, grid barrier,
+        update work) instead of two launches; same results."""
+        nat.check(self._lib.lbm_batch_set_cooperative(self._h, 1 if on else 0), "lbm_batch_set_cooperative")
+
+    def launch_shape(self):
+        """(phi-kernel nodes per thread, update-kernel threads per block)."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        nat.check(self._lib.lbm_batch_get_launch(self._h, ctypes.byref(a), ctypes.byref(b)), "lbm_batch_get_launch")
+        return int(a.value), int(b.value)
 
     def close(self):
         """Free the batch's tables (not the solvers)."""

@@ -472,6 +472,17 @@ class AllenCahnSolver:
                   "lbm_autotune")
         return (t[0], t[1], t[2]), float(ms.value)
 
+    def set_launch_shape(self, phi_nodes_per_thread, update_block):
+        """Launch shape of the two-kernel step (results do not depend on it)."""
+        nat.check(self._lib.lbm_set_launch(self._h, int(phi_nodes_per_thread), int(update_block)), "lbm_set_launch")
+
+    def launch_shape(self):
+        """(phi-kernel nodes per thread, update-kernel threads per block) of the
+        two-kernel step, as the autotuner left them."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        nat.check(self._lib.lbm_get_launch(self._h, ctypes.byref(a), ctypes.byref(b)), "lbm_get_launch")
+        return int(a.value), int(b.value)
+
     def set_tile(self, tx, ty, tz):
         """Step kernel selection: (0, 0, 0) the two-kernel streaming step (the
         default), else the fused tiled kernel with these tile extents."""

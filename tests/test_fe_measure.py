@@ -126,3 +126,35 @@ def test_device_measurements_from_concurrent_threads(ref, built_lib):
     for t in threads:
         t.join()
     assert not errors, errors[:2]
+
+
+@pytest.mark.parametrize("zc", [-3.0, 2.0, 7.5])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_wall_contact_angle_of_spherical_caps(built_lib, zc, dim):
+    """measure_contact_angle_wall on the spherical caps (radius 12, tanh
+    interface of width 4, centre height zc over the wall whose top layer is
+    z = 1): within 2 degrees of the cap's analytic angle in the first fluid
+    layer z = 2, cos(theta) = (2 - zc) / 12, with the library's own wall
+    normals and boundary mask (lbm_geometry_host: discrete normals of the flat
+    wall)."""
+    import ctypes
+    from lbm.fe_measure import measure_contact_angle_wall
+    phi, solid = inputs()[f"cap{dim}d_zc{zc}"]
+    shape = phi.shape
+    nx, ny, nz = shape if dim == 3 else (shape[0], shape[1], 1)
+    N = phi.size
+    bnd = np.empty(N, np.uint8)
+    wn = np.empty((dim, N), np.float32)
+    c = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rc = built_lib.lbm_geometry_host(nx, ny, nz, c(np.ascontiguousarray(solid).view(np.uint8)), None, 0, 120.0, 0.01,
+                                     0, None, c(bnd), c(wn), None, None, None)
+    assert rc == 0
+    theta = measure_contact_angle_wall(phi, solid, wn.reshape((dim,) + shape), bnd.reshape(shape))
+    assert theta == pytest.approx(np.degrees(np.arccos((2.0 - zc) / 12.0)), abs=2.0)
+
+
+def test_wall_contact_angle_without_contact():
+    from lbm.fe_measure import measure_contact_angle_wall
+    phi, solid = inputs()["cap3d_zc2.0"]
+    bnd = np.zeros(phi.shape, bool)
+    assert measure_contact_angle_wall(phi, solid, np.zeros((3,) + phi.shape, np.float32), bnd) == 180.0

@@ -140,3 +140,40 @@ def test_batch_with_amplification_field():
     plain = make(CASES[1], False)
     plain.run(6)
     assert not torch.equal(plain.phi, alone[0].phi)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
+def test_launch_shapes_give_identical_results(dtype):
+    """Every phi-kernel work size and update-kernel block the autotuners pick
+    from gives the same bits."""
+    ref = _solver(CASES[1], dtype)
+    ref.run(6)
+    for per, bs in ((4, 128), (12, 256), (32, 128)):
+        s = _solver(CASES[1], dtype)
+        s.set_launch_shape(per, bs)
+        assert s.launch_shape() == (per, bs)
+        s.run(6)
+        for x, y in zip(_state(ref), _state(s)):
+            assert torch.equal(x, y), (per, bs)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
+def test_cooperative_single_launch_matches_two_launches(dtype):
+    """The batched step as one cooperative launch (phi work, grid barrier,
+    update work) gives the two-launch step's results, mixing tau_f == 1 cases
+    with a tau_h = 0.57 case."""
+    from lbm.batch import AllenCahnBatch
+    taus = [None, 0.57, None, None]
+    two = [_solver(c, dtype, t) for c, t in zip(CASES, taus)]
+    one = [_solver(c, dtype, t) for c, t in zip(CASES, taus)]
+    b2, b1 = AllenCahnBatch(two), AllenCahnBatch(one)
+    b1.set_cooperative(True)
+    for n in (1, 5, 2):
+        b2.run(n)
+        b1.run(n)
+    torch.cuda.synchronize()
+    for a, m in zip(two, one):
+        for x, y in zip(_state(a), _state(m)):
+            assert torch.equal(x, y)
+    b1.close()
+    b2.close()
