@@ -15,7 +15,8 @@
 //   k_geo_bits     solid / partial / boundary bits of every node, the
 //                  near-wall distance seed (0 at boundary nodes, else 100)
 //   k_geo_smooth   wall normals -grad(frac)/|grad(frac)| times the boundary
-//                  mask (np.gradient stencil), every node (signed zeros kept)
+//                  mask (np.gradient stencil); off the boundary the signed
+//                  zero that product leaves
 //   k_geo_discrete wall normals from solid-neighbour counting (no fraction)
 //   k_geo_dist     one pass of the near-wall distance (11 passes)
 //   k_geo_final    class byte, top flag, next-interior node, fraction in the
@@ -138,17 +139,25 @@ __global__ void __launch_bounds__(kBlock) k_geo_smooth(GeoGrid g, const F* __res
   if (n >= g.N) return;
   int ix, iy, iz;
   gdecode(g, n, ix, iy, iz);
-  const F mask = (bits[n] & kBitBoundary) ? (F)1 : (F)0;
   const F g0 = grad_axis(g, frac, ix, iy, iz, 0);
   const F g1 = grad_axis(g, frac, ix, iy, iz, 1);
   const F g2 = g.two_d ? (F)0 : grad_axis(g, frac, ix, iy, iz, 2);
+  const size_t N = (size_t)g.N;
+  if (!(bits[n] & kBitBoundary)) {
+    // off the boundary the reference's (-g / |g|) * 0 is a zero with the sign
+    // of -g (|g| is clamped positive and the fraction has no NaN): no division
+    wn[n] = copysignf(0.0f, (float)-g0);
+    wn[N + n] = copysignf(0.0f, (float)-g1);
+    wn[2 * N + n] = g.two_d ? 0.0f : copysignf(0.0f, (float)-g2);
+    return;
+  }
+  const F mask = (F)1;
   F acc = (F)0;
   acc = r_add(acc, r_mul(g0, g0));
   acc = r_add(acc, r_mul(g1, g1));
   if (!g.two_d) acc = r_add(acc, r_mul(g2, g2));
   F mag = r_sqrt(acc);
   if (mag < (F)1e-10) mag = (F)1e-10;
-  const size_t N = (size_t)g.N;
   wn[n] = to_f32(r_mul(r_div(-g0, mag), mask));
   wn[N + n] = to_f32(r_mul(r_div(-g1, mag), mask));
   wn[2 * N + n] = g.two_d ? 0.0f : to_f32(r_mul(r_div(-g2, mag), mask));
