@@ -1,7 +1,8 @@
 """Golden fixture of the 150x150x107 ridge droplet-impact case (2000 steps).
 
 Runs pytorch-lbm's own AllenCahnSolver (imported read-only from --reference,
-CPU, 8 threads: ~40 min in float32, ~90 min in float64) on the drop-in GPU
+CPU, all host threads: about 40 min in float32 and several hours in float64
+on an 8-thread host) on the drop-in GPU
 case -- ridge R* = 1, R_d = 22.5 with smooth solid fraction, droplet R = 22.5 at
 (75, 75, 80), u = (0, 0, -0.05), theta = 162, alpha_geo = 1.5, sigma = 0.01424,
 tau_l = tau_g = 0.53, other solver arguments at their defaults -- and stores a

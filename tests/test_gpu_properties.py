@@ -94,8 +94,7 @@ def ensemble():
     and five one-ulp perturbations of them, float64 from the same inputs and
     three perturbations.  Every 50 steps: float64 sum of phi, Dx, Dy, Dz and
     the interface z-centre of each member; at the snapshot steps phi of every
-    float32 member and of the unperturbed float64 run, and u of both
-    unperturbed runs (on the host)."""
+    member, and u of both unperturbed runs (on the host)."""
     m32 = [_ridge(torch.float32)] + [_ridge_perturbed(seed) for seed in range(5)]
     m64 = [_ridge(torch.float64)] + [_ridge_perturbed(seed, torch.float64) for seed in range(3)]
     hist = {32: {}, 64: {}}
@@ -110,7 +109,7 @@ def ensemble():
             hist[bits][k] = np.array(rows)
         if k in SNAPS:
             snaps[k] = {"phi32": [m.phi.double().cpu().numpy() for m in m32],
-                        "phi64": m64[0].phi.cpu().numpy(),
+                        "phi64": [m.phi.cpu().numpy() for m in m64],
                         "u32": m32[0].u.double().cpu().numpy(), "u64": m64[0].u.cpu().numpy()}
     status = [m.status() for m in m32 + m64]
     for m in m32 + m64:
@@ -132,29 +131,33 @@ def _check_history(ref_hist, env):
         assert lo[4] - span[4] - 0.05 <= row[6] <= hi[4] + span[4] + 0.05, (k, row[6], lo[4], hi[4])
 
 
-def test_reference_history_within_perturbation_ensemble(ensemble):
+@pytest.mark.parametrize("dtype_name,bits", [("float32", 32), ("float64", 64)])
+def test_reference_history_within_perturbation_ensemble(ensemble, dtype_name, bits):
     """sum(phi), spread extents and interface z-centre of the reference's own
-    float32 run of the whole case (2000 steps), every 50 steps, lie inside the
-    envelope of GPU float32 runs whose inputs differ by one float32 ulp (the
-    spread a rounding-level difference produces in this case)."""
-    ref = _ref150("float32")
+    run of the whole case (2000 steps) in float32 and in float64, every 50
+    steps, lie inside the envelope of the GPU runs of the same precision whose
+    inputs differ by one ulp of it (the spread a rounding-level difference
+    produces in this case)."""
+    ref = _ref150(dtype_name)
     assert int(ref["hist"][-1, 0]) == STEPS and len(ref["hist"]) == STEPS // 50
-    _check_history(ref["hist"], ensemble["hist"][32])
+    _check_history(ref["hist"], ensemble["hist"][bits])
     assert all(st == 0 for st in ensemble["status"])
 
 
-@pytest.mark.parametrize("dtype_name", ["float32"])
+@pytest.mark.parametrize("dtype_name", ["float32", "float64"])
 def test_reference_fields_within_perturbation_spread(ensemble, dtype_name):
     """phi of the reference's run at steps 100, 500 and 2000 (stored to 1.5e-5)
-    is no farther from the GPU run than one-ulp perturbed GPU runs are from
-    each other (the largest distance among the float32 members, with half
-    again as margin: six samples of a spread), and the norm of u within 1 %."""
+    is no farther from the GPU run of the same precision than one-ulp
+    perturbed GPU runs are from each other (the largest distance among the
+    members, with half again as margin: a few samples of a spread), and the
+    norm of u within 1 %."""
     ref = _ref150(dtype_name)
+    key = "phi32" if dtype_name == "float32" else "phi64"
     for k in SNAPS:
         sn = ensemble["snaps"][k]
-        members = sn["phi32"]
+        members = sn[key]
         spread = max(np.abs(a - b).max() for i, a in enumerate(members) for b in members[i + 1:])
-        ours = sn["phi32"][0] if dtype_name == "float32" else sn["phi64"]
+        ours = members[0]
         ref_phi = ref[f"s{k}_phi_q"].astype(np.float64) / 65535.0
         d = np.abs(ours - ref_phi).max()
         assert d <= 1.5 * spread + 2e-5, (k, d, spread)
@@ -195,7 +198,7 @@ def test_float32_against_float64_instance(ensemble):
         sn = ensemble["snaps"][k]
         base = sn["phi32"][0]
         dulp = max(np.abs(base - m).max() for m in sn["phi32"][1:])
-        d64 = np.abs(base - sn["phi64"]).max()
+        d64 = np.abs(base - sn["phi64"][0]).max()
         assert d64 <= 1.5 * dulp, (k, d64, dulp)
     for k, e32 in ensemble["hist"][32].items():
         e64 = ensemble["hist"][64][k]
