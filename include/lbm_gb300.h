@@ -106,8 +106,22 @@ typedef struct LbmHandle LbmHandle;
 int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz,
                int precision, LbmHandle** out);
 
-/* Free the handle and its device memory. */
+/* Free the handle.  Waits for the device's queued work (as cudaFree does),
+ * then returns the grid's state arrays to the process's cache of device
+ * blocks, from which lbm_create takes blocks of a fitting size (at most 1/8
+ * larger, same device) before it allocates; past the cache's limit they are
+ * freed.  The reference frees its tensors through PyTorch's caching
+ * allocator, which keeps them likewise. */
 int lbm_destroy(LbmHandle* h);
+
+/* The cache of state arrays: its limit in bytes (default 16 GiB; 0 frees
+ * every cached block and disables caching), freeing every cached block
+ * (`freed_bytes` may be NULL), and the bytes it holds.  lbm_create also
+ * empties it and retries when cudaMalloc runs out of memory.  No reference
+ * counterpart (torch.cuda.empty_cache for the reference's tensors). */
+int lbm_cache_limit(uint64_t bytes);
+int lbm_cache_trim(uint64_t* freed_bytes);
+int lbm_cache_bytes(uint64_t* cached_bytes);
 
 /* Solid mask (host, N bytes, nonzero = solid) and optional solid fraction
  * (host, N elements of fraction_dtype, or NULL with LBM_DT_NONE).  Computes
@@ -142,7 +156,11 @@ int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype);
  * 2N on a 2-D grid; NULL = zero), of element type src_dtype, in host memory (on_device = 0) or
  * device memory (on_device = 1).  Sets f = f_eq(phi, u), g = g_eq(0, u) and
  * the phi-mass reference.  Replaces AllenCahnSolver.init_fields
- * (lbm/fe_ac_solver.py:239-261).  Asynchronous on `stream`. */
+ * (lbm/fe_ac_solver.py:239-261).  Asynchronous on `stream` for device
+ * inputs.  Host inputs may be released when the call returns: where the
+ * device reads pageable host memory in place (cudaDevAttrPageableMemoryAccess,
+ * a Grace host), the kernel reads them without a staging copy and the call
+ * waits for it; elsewhere they are copied to the device first. */
 int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
                     int on_device, void* stream);
 

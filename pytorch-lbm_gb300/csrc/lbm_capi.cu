@@ -8,8 +8,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/lbm_gb300.h"
@@ -370,12 +372,107 @@ Tiling make_tiling(int64_t nx, int64_t ny, int64_t nz, int tx, int ty, int tz, i
   return tiling_of(nx, ny, nz, tx > 0 ? tx : 6, ty > 0 ? ty : 6, tz);
 }
 
+// ---------------------------------------------------------------------------
+// Cache of state arrays.  lbm_destroy hands the state arrays of a grid back
+// to a per-process cache instead of cudaFree, and lbm_create takes blocks of
+// a fitting size (at most 1/8 larger) on the same device from it before it
+// calls cudaMalloc: a sweep or a serving loop that opens and closes grids of
+// recurring sizes then neither maps nor unmaps device memory per grid.  The
+// cache holds at most g_cache_limit bytes (lbm_cache_limit; 0 disables it);
+// a cudaMalloc that runs out of memory empties it and retries.  Recycled
+// blocks hold old data: every array is written (memset or kernels) before it
+// is read, as with fresh cudaMalloc memory, which CUDA does not zero either.
+// ---------------------------------------------------------------------------
+struct CachedBlock {
+  int device;
+  size_t bytes;
+  void* p;
+};
+std::mutex g_cache_mu;
+std::vector<CachedBlock> g_cache;                    // free blocks
+std::unordered_map<void*, CachedBlock> g_cache_live; // blocks handed out
+size_t g_cache_bytes = 0;
+size_t g_cache_limit = (size_t)16 << 30;
+
+void cache_trim_locked(int device) {
+  for (size_t i = 0; i < g_cache.size();) {
+    if (device < 0 || g_cache[i].device == device) {
+      cudaFree(g_cache[i].p);
+      g_cache_bytes -= g_cache[i].bytes;
+      g_cache[i] = g_cache.back();
+      g_cache.pop_back();
+    } else {
+      ++i;
+    }
+  }
+}
+
+cudaError_t cache_alloc(void** p, size_t bytes, int device) {
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    int best = -1;
+    for (int i = 0; i < (int)g_cache.size(); ++i) {
+      const CachedBlock& b = g_cache[i];
+      if (b.device == device && b.bytes >= bytes && b.bytes - bytes <= bytes / 8 &&
+          (best < 0 || b.bytes < g_cache[best].bytes))
+        best = i;
+    }
+    if (best >= 0) {
+      const CachedBlock b = g_cache[best];
+      g_cache[best] = g_cache.back();
+      g_cache.pop_back();
+      g_cache_bytes -= b.bytes;
+      g_cache_live[b.p] = b;
+      *p = b.p;
+      return cudaSuccess;
+    }
+  }
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaErrorMemoryAllocation) {
+    (void)cudaGetLastError();
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    cache_trim_locked(device);
+    e = cudaMalloc(p, bytes);
+  }
+  if (e == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_cache_live[*p] = CachedBlock{device, bytes, *p};
+  }
+  return e;
+}
+
+// Returns a block from cache_alloc to the cache (or frees it past the
+// limit); frees anything else.  The caller has synchronised the device.
+void cache_release(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  auto it = g_cache_live.find(p);
+  if (it == g_cache_live.end()) {
+    cudaFree(p);
+    return;
+  }
+  const CachedBlock b = it->second;
+  g_cache_live.erase(it);
+  if (g_cache_bytes + b.bytes <= g_cache_limit) {
+    g_cache.push_back(b);
+    g_cache_bytes += b.bytes;
+  } else {
+    cudaFree(p);
+  }
+}
+
 void free_all(LbmHandle* h) {
   void* ptrs[] = {h->f[0], h->f[1], h->g[0], h->g[1], h->u,        h->phi[0], h->phi[1], h->eps,
                   h->cls,  h->wn,   h->partials, h->counters, h->cbuf, h->scal, h->meas_phi, h->desc,
                   h->amp,  h->mu, h->gmu, h->nsw, h->cubic};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
+  // kernels still queued on any stream may use the arrays (cudaFree would
+  // wait for them as well)
+  int cur = 0;
+  if (cudaGetDevice(&cur) == cudaSuccess && cudaSetDevice(h->device) == cudaSuccess) {
+    cudaDeviceSynchronize();
+    cudaSetDevice(cur);
+  }
+  for (void* p : ptrs) cache_release(p);
 }
 
 template <typename T>
@@ -656,7 +753,7 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz, int 
   const Sizes z = sizes_of(nx, ny, nz, precision);
   cudaError_t e = cudaSuccess;
   auto A = [&](void** p, size_t bytes) {
-    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) e = cache_alloc(p, bytes, h->device);
   };
   for (int b = 0; b < 2; ++b) {
     A(&h->f[b], z.pop);
@@ -698,10 +795,38 @@ int lbm_destroy(LbmHandle* h) {
   return LBM_OK;
 }
 
+int lbm_cache_limit(uint64_t bytes) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  g_cache_limit = (size_t)bytes;
+  if (g_cache_bytes > g_cache_limit) cache_trim_locked(-1);
+  return LBM_OK;
+}
+
+int lbm_cache_trim(uint64_t* freed_bytes) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  const size_t before = g_cache_bytes;
+  cache_trim_locked(-1);
+  if (freed_bytes) *freed_bytes = before - g_cache_bytes;
+  return LBM_OK;
+}
+
+int lbm_cache_bytes(uint64_t* cached_bytes) {
+  if (!cached_bytes) return fail(LBM_E_ARG, "lbm_cache_bytes: null argument");
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  *cached_bytes = g_cache_bytes;
+  return LBM_OK;
+}
+
 namespace {
+// Scratch of launch_geometry: three N-byte planes (bits, distance, its
+// transform), then at the next 256-byte boundary the boundary-node count (256
+// bytes reserved) and list (N ints).
+size_t geo_scratch_bytes(size_t N) { return ((3 * N + 255) & ~(size_t)255) + 256 + 4 * N; }
+
 // The device geometry precompute of a handle from device copies of the
 // solid mask and fraction, then the constant tables; asynchronous on `st`.
-// scratch: 2 N device bytes the kernels may use.
+// scratch: geo_scratch_bytes(N) device bytes the kernels may use, 256-byte
+// aligned.
 int set_geometry_device(LbmHandle* h, const uint8_t* solid, const void* fraction, int fraction_dtype,
                         uint8_t* scratch, cudaStream_t st) {
   const int64_t N = h->N;
@@ -757,11 +882,13 @@ int lbm_set_geometry(LbmHandle* h, const uint8_t* solid, const void* fraction, i
     return fail(LBM_E_ARG, "lbm_set_geometry: fraction and fraction_dtype disagree");
   // the inputs are staged through the population buffer the next step
   // writes (it holds no state between steps): solid (N bytes), the fraction
-  // (N elements), then the kernels' 2 N bytes of scratch
+  // (N elements), then the kernels' scratch
   const size_t N = (size_t)h->N;
   const size_t fb = fraction_dtype == 0 ? 0 : N * (fraction_dtype == 1 ? 4 : 8);
   uint8_t* stage = static_cast<uint8_t*>(h->f[h->cur ^ 1]);
   const size_t off_f = (N + 255) & ~(size_t)255, off_s = (off_f + fb + 255) & ~(size_t)255;
+  if (off_s + geo_scratch_bytes(N) > (size_t)nq_of(h->nz) * h->Np * h->psize)
+    return fail(LBM_E_ARG, "lbm_set_geometry: internal error: staging exceeds the population buffer");
   CUDA_TRY(cudaMemcpyAsync(stage, solid, N, cudaMemcpyHostToDevice, 0));
   if (fb) CUDA_TRY(cudaMemcpyAsync(stage + off_f, fraction, fb, cudaMemcpyHostToDevice, 0));
   const int rc = set_geometry_device(h, stage, fb ? stage + off_f : nullptr, fraction_dtype, stage + off_s, 0);
@@ -776,6 +903,8 @@ int lbm_set_geometry_device(LbmHandle* h, const uint8_t* solid, const void* frac
   if (!h || !solid) return fail(LBM_E_ARG, "lbm_set_geometry_device: null argument");
   if (fraction_dtype < 0 || fraction_dtype > 2 || ((fraction_dtype != 0) != (fraction != nullptr)))
     return fail(LBM_E_ARG, "lbm_set_geometry_device: fraction and fraction_dtype disagree");
+  if (geo_scratch_bytes((size_t)h->N) > (size_t)nq_of(h->nz) * h->Np * h->psize)
+    return fail(LBM_E_ARG, "lbm_set_geometry_device: internal error: scratch exceeds the population buffer");
   return set_geometry_device(h, solid, fraction, fraction_dtype, static_cast<uint8_t*>(h->f[h->cur ^ 1]),
                              static_cast<cudaStream_t>(stream));
 }
@@ -811,6 +940,28 @@ int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype) {
   return LBM_OK;
 }
 
+namespace {
+// Whether kernels on `device` may read pageable host memory in place
+// (cudaDevAttrPageableMemoryAccess: a Grace host with address translation
+// services reaches it over the chip-to-chip link).  Cached per device.
+bool pageable_direct(int device) {
+  static std::mutex mu;
+  static std::vector<int> known;  // -1 unknown, 0 no, 1 yes
+  std::lock_guard<std::mutex> lk(mu);
+  if (device < 0) return false;
+  if ((int)known.size() <= device) known.resize(device + 1, -1);
+  if (known[device] < 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+      (void)cudaGetLastError();
+      v = 0;
+    }
+    known[device] = v ? 1 : 0;
+  }
+  return known[device] == 1;
+}
+}  // namespace
+
 int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype, int on_device, void* stream) {
   NvtxRange range("lbm_init_fields");
   if (!h || !phi) return fail(LBM_E_ARG, "lbm_init_fields: null argument");
@@ -819,12 +970,16 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const size_t es = src_dtype == LBM_DT_F32 ? 4 : 8;
   const int64_t N = h->N;
-  // Host inputs are staged through the (not yet used) second g buffer:
-  // 19 N T-elements hold the 4 N source elements.
+  // Host inputs are read by the kernel in place where the device reaches
+  // pageable host memory (the call then waits for the kernel, so that the
+  // caller may free them on return as after a copy); elsewhere they are
+  // staged through the (not yet used) second g buffer: 19 N T-elements hold
+  // the 4 N source elements.
   int in = h->cur;
   const void* dphi = phi;
   const void* du = u;
-  if (!on_device) {
+  const bool direct = !on_device && pageable_direct(h->device);
+  if (!on_device && !direct) {
     char* stage = static_cast<char*>(h->g[in ^ 1]);
     CUDA_TRY(cudaMemcpyAsync(stage, phi, N * es, cudaMemcpyHostToDevice, st));
     dphi = stage;
@@ -848,6 +1003,7 @@ int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
                : launch_init<T, S, double>(consts_of<T>(*h), s, (const double*)dphi, (const double*)du, st);
   });
   if (e != cudaSuccess) return fail(LBM_E_CUDA, std::string("lbm_init_fields: ") + cudaGetErrorString(e));
+  if (direct) CUDA_TRY(cudaStreamSynchronize(st));
   h->initialized = true;
   h->desc_ok = false;
   h->raw = true;

@@ -28,6 +28,7 @@ EXPORTS = (
     "lbm_footprint",
     "lbm_batch_create", "lbm_batch_step", "lbm_batch_size", "lbm_batch_autotune", "lbm_batch_destroy",
     "lbm_set_launch", "lbm_get_launch", "lbm_batch_get_launch", "lbm_batch_set_cooperative",
+    "lbm_cache_limit", "lbm_cache_trim", "lbm_cache_bytes",
     "lbm_inject_droplet", "lbm_set_amplification", "lbm_state_bytes", "lbm_save_state", "lbm_load_state",
     "lbm_write_vtk", "lbm_reduce",
 )
@@ -81,6 +82,9 @@ def _declare(L):
         "lbm_get_launch": ([_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], _i32),
         "lbm_batch_get_launch": ([_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], _i32),
         "lbm_batch_set_cooperative": ([_vp, _i32], _i32),
+        "lbm_cache_limit": ([ctypes.c_uint64], _i32),
+        "lbm_cache_trim": ([_vp], _i32),
+        "lbm_cache_bytes": ([_vp], _i32),
         "lbm_inject_droplet": ([_vp, ctypes.POINTER(_dbl), _dbl, _dbl, ctypes.POINTER(_dbl), ctypes.POINTER(_i64),
                                 _vp], _i32),
         "lbm_set_amplification": ([_vp, _vp, _i32], _i32),
@@ -138,3 +142,22 @@ def ptr(t):
 def stream_ptr(stream=None):
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
+
+
+def cache_limit(nbytes):
+    """Limit of the library's cache of grid state arrays (0 disables it)."""
+    check(lib().lbm_cache_limit(int(nbytes)), "lbm_cache_limit")
+
+
+def cache_trim():
+    """Free every cached state array; returns the bytes freed."""
+    n = ctypes.c_uint64()
+    check(lib().lbm_cache_trim(ctypes.byref(n)), "lbm_cache_trim")
+    return int(n.value)
+
+
+def cache_bytes():
+    """Bytes of device memory the cache holds."""
+    n = ctypes.c_uint64()
+    check(lib().lbm_cache_bytes(ctypes.byref(n)), "lbm_cache_bytes")
+    return int(n.value)

@@ -117,3 +117,14 @@ def test_device_tables_match_host_tables(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.strip() == "0"
+
+
+def test_cache_entry_points_without_a_gpu(built_lib):
+    """The state-array cache is empty in a process that made no grid: its
+    size, trim and limit need no device."""
+    from lbm import _native as nat
+    assert nat.cache_bytes() == 0
+    assert nat.cache_trim() == 0
+    nat.cache_limit(0)
+    nat.cache_limit(16 << 30)
+    assert built_lib.lbm_cache_bytes(None) != 0  # null output pointer rejected
