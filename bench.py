@@ -336,22 +336,31 @@ def run_ours(args, rank, world, device):
     s.close()
 
     # --- end to end through the public API from host arrays ----------------
-    torch.cuda.synchronize(device)
-    barrier(world)
-    t0 = time.perf_counter()
-    s2 = AllenCahnSolver(cfg, dtype=pdt, **skw)
-    s2.set_solid(solid, frac)
-    s2.init_fields(C, u)
-    reads = 0
-    for k in range(1, K + 1):
-        s2.step()
-        if k % 50 == 0:
-            _ = s2.phi.cpu().numpy()
-            reads += 1
-    m2 = s2.measure()
-    torch.cuda.synchronize(device)
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, world, device)
+    # the whole solve (construct, set-up from host arrays, K steps with phi to
+    # the host every 50 steps, measure) is repeated like the timed region:
+    # until ~0.5 s have passed (at most 5 times); the median is reported
+    e2e_reps = []
+    while True:
+        torch.cuda.synchronize(device)
+        barrier(world)
+        t0 = time.perf_counter()
+        s2 = AllenCahnSolver(cfg, dtype=pdt, **skw)
+        s2.set_solid(solid, frac)
+        s2.init_fields(C, u)
+        reads = 0
+        for k in range(1, K + 1):
+            s2.step()
+            if k % 50 == 0:
+                _ = s2.phi.cpu().numpy()
+                reads += 1
+        m2 = s2.measure()
+        torch.cuda.synchronize(device)
+        e2e_reps.append(max_over_ranks(time.perf_counter() - t0, world, device))
+        more = sum(e2e_reps) < 0.5 and len(e2e_reps) < 5
+        if not bcast_flag(more, world, device):
+            break
+        s2.close()
+    e2e_s = statistics.median(e2e_reps)
     s2_fields = [x.double().cpu().numpy() for x in s2.fields("phi", "u")]
     s2_meas = dict(m2, phi_mass_init=s2.phi_mass_init)
     s2.close()
@@ -431,8 +440,10 @@ def run_ours(args, rank, world, device):
             "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
                     "d2h_bytes_per_step": d2h / K,
                     "what": f"AllenCahnSolver from host arrays: create + set_solid + init_fields + {K} steps "
-                            f"+ phi to host every 50 steps + measure; {e2e_s:.3f} s; the state arrays come "
+                            f"+ phi to host every 50 steps + measure; median of {len(e2e_reps)} repetitions "
+                            f"{e2e_s * 1e3:.2f} ms (first {e2e_reps[0] * 1e3:.2f} ms); the state arrays come "
                             "from the library's cache (the timed solver's, closed before)",
+                    "reps_ms": [round(x * 1e3, 3) for x in e2e_reps],
                     "device_diagnostics": {
                         "value": replica_mlups(n, K, e2e_m_s * 1e3, world), "unit": "MLUPS",
                         "d2h_bytes_per_step": (K // 50) * 9 * 8 / K,
