@@ -394,10 +394,15 @@ std::unordered_map<void*, CachedBlock> g_cache_live; // blocks handed out
 size_t g_cache_bytes = 0;
 size_t g_cache_limit = (size_t)16 << 30;
 
+// Frees the cached blocks of `device` (every device for -1), each with its
+// own device current.
 void cache_trim_locked(int device) {
+  if (g_cache.empty()) return;
+  int cur = -1;
+  (void)cudaGetDevice(&cur);
   for (size_t i = 0; i < g_cache.size();) {
     if (device < 0 || g_cache[i].device == device) {
-      cudaFree(g_cache[i].p);
+      if (cudaSetDevice(g_cache[i].device) == cudaSuccess) cudaFree(g_cache[i].p);
       g_cache_bytes -= g_cache[i].bytes;
       g_cache[i] = g_cache.back();
       g_cache.pop_back();
@@ -405,6 +410,7 @@ void cache_trim_locked(int device) {
       ++i;
     }
   }
+  if (cur >= 0) (void)cudaSetDevice(cur);
 }
 
 cudaError_t cache_alloc(void** p, size_t bytes, int device) {
@@ -466,13 +472,14 @@ void free_all(LbmHandle* h) {
                   h->cls,  h->wn,   h->partials, h->counters, h->cbuf, h->scal, h->meas_phi, h->desc,
                   h->amp,  h->mu, h->gmu, h->nsw, h->cubic};
   // kernels still queued on any stream may use the arrays (cudaFree would
-  // wait for them as well)
-  int cur = 0;
-  if (cudaGetDevice(&cur) == cudaSuccess && cudaSetDevice(h->device) == cudaSuccess) {
-    cudaDeviceSynchronize();
-    cudaSetDevice(cur);
-  }
+  // wait for them as well); the handle's device is current while they are
+  // released
+  int cur = -1;
+  (void)cudaGetDevice(&cur);
+  const bool on_dev = cudaSetDevice(h->device) == cudaSuccess;
+  if (on_dev) cudaDeviceSynchronize();
   for (void* p : ptrs) cache_release(p);
+  if (on_dev && cur >= 0) (void)cudaSetDevice(cur);
 }
 
 template <typename T>
