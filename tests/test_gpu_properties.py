@@ -88,17 +88,20 @@ def test_first_steps_vs_oracle_full_size():
 
 STEPS = 2000
 SNAPS = (100, 500, 2000)
+MEMBERS = 12       # runs per precision in the one-ulp ensemble
+SNAP_MEMBERS = 6   # of which phi is kept at the snapshot steps
 
 
 @pytest.fixture(scope="module")
 def ensemble():
-    """The full 2000-step run on the GPU: float32 from the generator's inputs
-    and five one-ulp perturbations of them, float64 from the same inputs and
-    three perturbations.  Every 50 steps: float64 sum of phi, Dx, Dy, Dz and
-    the interface z-centre of each member; at the snapshot steps phi of every
-    member, and u of both unperturbed runs (on the host)."""
-    m32 = [_ridge(torch.float32)] + [_ridge_perturbed(seed) for seed in range(5)]
-    m64 = [_ridge(torch.float64)] + [_ridge_perturbed(seed, torch.float64) for seed in range(3)]
+    """The full 2000-step run on the GPU, in float32 and in float64: from the
+    generator's inputs and from eleven one-ulp perturbations of them in each
+    precision.  Every 50 steps: float64 sum of phi, Dx, Dy, Dz and the
+    interface z-centre of each member; at the snapshot steps phi of the first
+    SNAP_MEMBERS members of each precision, and u of both unperturbed runs (on
+    the host)."""
+    m32 = [_ridge(torch.float32)] + [_ridge_perturbed(seed) for seed in range(MEMBERS - 1)]
+    m64 = [_ridge(torch.float64)] + [_ridge_perturbed(seed, torch.float64) for seed in range(MEMBERS - 1)]
     hist = {32: {}, 64: {}}
     snaps = {}
     for k in range(50, STEPS + 1, 50):
@@ -110,8 +113,8 @@ def ensemble():
                 rows.append((float(m.phi.double().sum()), d["Dx"], d["Dy"], d["Dz"], d["z_com"]))
             hist[bits][k] = np.array(rows)
         if k in SNAPS:
-            snaps[k] = {"phi32": [m.phi.double().cpu().numpy() for m in m32],
-                        "phi64": [m.phi.cpu().numpy() for m in m64],
+            snaps[k] = {"phi32": [m.phi.double().cpu().numpy() for m in m32[:SNAP_MEMBERS]],
+                        "phi64": [m.phi.cpu().numpy() for m in m64[:SNAP_MEMBERS]],
                         "u32": m32[0].u.double().cpu().numpy(), "u64": m64[0].u.cpu().numpy()}
     status = [m.status() for m in m32 + m64]
     for m in m32 + m64:
@@ -120,14 +123,22 @@ def ensemble():
 
 
 def _check_history(ref_hist, env):
+    """The reference's row at every checkpoint against the ensemble's members
+    there: sum(phi) within three standard deviations of the members' mean,
+    the deviation widened by 2e-6 relative (the reference sums phi for its
+    mass correction in its own precision and order, which moves its sum by
+    ~1e-7 relative from the first steps on); Dx, Dy, Dz within the members'
+    range +- 1 node; the z-centre within their range widened by its width and
+    0.05.  The reference's run is one more run with rounding-level different
+    arithmetic, i.e. one more draw from the distribution the members sample."""
     for row in ref_hist:
         k = int(row[0])
         e = env[k]
         lo, hi = e.min(0), e.max(0)
         span = hi - lo
-        # mass: envelope widened by its own width and 2e-6 relative
-        tol_m = span[0] + 2e-6 * abs(row[1])
-        assert lo[0] - tol_m <= row[1] <= hi[0] + tol_m, (k, row[1], lo[0], hi[0])
+        mean, sd = e[:, 0].mean(), e[:, 0].std(ddof=1)
+        tol_m = 3.0 * (sd + 2e-6 * abs(row[1]))
+        assert abs(row[1] - mean) <= tol_m, (k, row[1], mean, sd)
         for j, col in ((1, 2), (2, 3), (3, 4)):  # Dx, Dy, Dz within the envelope +- 1 node
             assert lo[j] - 1 <= row[col] <= hi[j] + 1, (k, j, row[col], lo[j], hi[j])
         assert lo[4] - span[4] - 0.05 <= row[6] <= hi[4] + span[4] + 0.05, (k, row[6], lo[4], hi[4])
@@ -137,9 +148,9 @@ def _check_history(ref_hist, env):
 def test_reference_history_within_perturbation_ensemble(ensemble, dtype_name, bits):
     """sum(phi), spread extents and interface z-centre of the reference's own
     run of the whole case (2000 steps) in float32 and in float64, every 50
-    steps, lie inside the envelope of the GPU runs of the same precision whose
-    inputs differ by one ulp of it (the spread a rounding-level difference
-    produces in this case)."""
+    steps, lie within the spread of the twelve GPU runs of the same precision
+    whose initial phi differ by one float32 ulp (the spread a rounding-level
+    difference produces in this case)."""
     ref = _ref150(dtype_name)
     assert int(ref["hist"][-1, 0]) == STEPS and len(ref["hist"]) == STEPS // 50
     _check_history(ref["hist"], ensemble["hist"][bits])
