@@ -240,14 +240,17 @@ def run_reference_arm(args, rank, world):
     name = args.workload
     out = None
     if rank == 0:
-        # bounded sample: at most 4 timed steps (each ~3-4 s of one core at 2.4 M nodes)
+        # bounded sample: K timed steps of the full grid, at most --ref-steps of
+        # them (1.3-5 s each on one core at 2.4 M nodes), after up to 3 warm-up steps
         steps = max(1, min(args.steps, args.ref_steps))
-        mlups, dt = cpu_oracle_mlups(name, steps, warmup=min(args.warmup, 1))
+        wu = min(args.warmup, 3)
+        mlups, dt = cpu_oracle_mlups(name, steps, warmup=wu)
         w = WORKLOADS[name]
         n = int(np.prod(w["grid"]))
-        sample = f"{steps} timed steps (+1 warm-up) of the full {w['grid'][0]}x{w['grid'][1]}x{w['grid'][2]} grid"
+        sample = (f"{steps} timed steps (+{wu} warm-up) of the full {w['grid'][0]}x{w['grid'][1]}x{w['grid'][2]} "
+                  "grid")
         out = {"impl": "reference", "metric": "MLUPS", "value": mlups, "unit": "MLUPS", "n_gpus": world,
-               "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / steps * 1e3,
+               "steps": steps, "warmup": wu, "ms_per_step": dt / steps * 1e3,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic", "config": {"workload": w["label"], "nodes": n, "precision": "fp32"},
                "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": 1, "kind": "port",
@@ -740,7 +743,7 @@ def main():
     ap.add_argument("--serve-saturate", type=float, default=4e6,
                     help="nodes per tick of the shortest-remaining-work-first serving policy")
     ap.add_argument("--cpu-steps", type=int, default=3)
-    ap.add_argument("--ref-steps", type=int, default=4)
+    ap.add_argument("--ref-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true", help="skip the float64 run of the same workload")
     ap.add_argument("--min-seconds", type=float, default=0.5,
