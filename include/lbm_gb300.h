@@ -160,7 +160,8 @@ int lbm_set_amplification(LbmHandle* h, const void* alpha, int alpha_dtype);
  * inputs.  Host inputs may be released when the call returns: where the
  * device reads pageable host memory in place (cudaDevAttrPageableMemoryAccess,
  * a Grace host), the kernel reads them without a staging copy and the call
- * waits for it; elsewhere they are copied to the device first. */
+ * waits for it; elsewhere, or with LBM_HOST_STAGING=1 in the environment,
+ * they are copied to the device first. */
 int lbm_init_fields(LbmHandle* h, const void* phi, const void* u, int src_dtype,
                     int on_device, void* stream);
 

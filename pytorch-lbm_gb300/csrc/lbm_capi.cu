@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -951,11 +952,17 @@ namespace {
 // Whether kernels on `device` may read pageable host memory in place
 // (cudaDevAttrPageableMemoryAccess: a Grace host with address translation
 // services reaches it over the chip-to-chip link).  Cached per device.
+// LBM_HOST_STAGING=1 in the environment selects the staging copy on every
+// device.
 bool pageable_direct(int device) {
   static std::mutex mu;
   static std::vector<int> known;  // -1 unknown, 0 no, 1 yes
+  static const bool staging = [] {
+    const char* v = std::getenv("LBM_HOST_STAGING");
+    return v && v[0] == '1';
+  }();
   std::lock_guard<std::mutex> lk(mu);
-  if (device < 0) return false;
+  if (device < 0 || staging) return false;
   if ((int)known.size() <= device) known.resize(device + 1, -1);
   if (known[device] < 0) {
     int v = 0;

@@ -112,3 +112,33 @@ def test_cache_accounting_limit_and_trim():
     assert held - nat.cache_bytes() <= 256 << 10 < footprint(CASES["flat_q120"]["grid"], torch.float32)
     s.close()
     nat.cache_trim()
+
+
+def test_host_inputs_read_in_place_equal_staged_copy(tmp_path):
+    """init_fields from host arrays gives the same state whether the kernel
+    reads them in place (the default where the device reaches pageable host
+    memory) or from a staging copy (LBM_HOST_STAGING=1, in a child process)."""
+    import os
+    import subprocess
+    import sys
+    script = tmp_path / "run.py"
+    tests = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(tests)
+    paths = [root, os.path.join(root, "pytorch-lbm_gb300"), tests, os.path.join(tests, "golden")]
+    script.write_text(
+        "import sys, numpy as np, torch\n"
+        f"sys.path[:0] = {paths!r}\n"
+        "import test_gpu_cache as t\n"
+        "out = t._run('ridge_l162', torch.float32, 6)\n"
+        "np.savez(sys.argv[1], *[x.cpu().numpy() for x in out])\n")
+    env = dict(os.environ)
+    res = []
+    for staging in ("0", "1"):
+        env["LBM_HOST_STAGING"] = staging
+        path = tmp_path / f"s{staging}.npz"
+        subprocess.run([sys.executable, str(script), str(path)], env=env, check=True, timeout=600)
+        import numpy as np
+        d = np.load(path)
+        res.append([d[k] for k in sorted(d.files)])
+    for a, b in zip(*res):
+        assert a.tobytes() == b.tobytes()
