@@ -17,7 +17,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 # scripts/validate_solver.py:24-38
-BASELINE = {"k": 1.2963, "z_com": 17.6, "Dx": 35.0, "Dy": 27.0}
+VALIDATION_VALUES = {"k": 1.2963, "z_com": 17.6, "Dx": 35.0, "Dy": 27.0}
 TOLERANCE = {"k": 0.05, "z_com": 1.0, "Dx": 2.0, "Dy": 2.0}
 
 
@@ -60,7 +60,7 @@ def test_reference_validation_case():
     s.run(500)
     m = s.measure()
     got = {"k": m["k"], "z_com": m["z_com"], "Dx": m["Dx"], "Dy": m["Dy"]}
-    for key, ref in BASELINE.items():
+    for key, ref in VALIDATION_VALUES.items():
         assert abs(got[key] - ref) <= TOLERANCE[key], (key, got[key], ref)
     phi = s.phi
     assert abs(float(phi.sum()) - m0) / m0 <= 1e-4
