@@ -94,18 +94,19 @@ SNAP_MEMBERS = 6   # of which phi is kept at the snapshot steps
 
 @pytest.fixture(scope="module")
 def ensemble():
-    """The full 2000-step run on the GPU, in float32 and in float64: from the
-    generator's inputs and from eleven one-ulp perturbations of them in each
-    precision.  Every 50 steps: float64 sum of phi, Dx, Dy, Dz and the
+    """The full 2000-step run on the GPU, in float32, in float64 and with
+    half-precision population storage: from the generator's inputs and from
+    eleven one-ulp perturbations of them in each form.  Every 50 steps: float64 sum of phi, Dx, Dy, Dz and the
     interface z-centre of each member; at the snapshot steps phi of the first
     SNAP_MEMBERS members of each precision, and u of both unperturbed runs (on
     the host)."""
     m32 = [_ridge(torch.float32)] + [_ridge_perturbed(seed) for seed in range(MEMBERS - 1)]
     m64 = [_ridge(torch.float64)] + [_ridge_perturbed(seed, torch.float64) for seed in range(MEMBERS - 1)]
-    hist = {32: {}, 64: {}}
+    m16 = [_ridge(torch.float16)] + [_ridge_perturbed(seed, torch.float16) for seed in range(MEMBERS - 1)]
+    hist = {32: {}, 64: {}, 16: {}}
     snaps = {}
     for k in range(50, STEPS + 1, 50):
-        for bits, members in ((32, m32), (64, m64)):
+        for bits, members in ((32, m32), (64, m64), (16, m16)):
             rows = []
             for m in members:
                 m.run(50)
@@ -116,8 +117,8 @@ def ensemble():
             snaps[k] = {"phi32": [m.phi.double().cpu().numpy() for m in m32[:SNAP_MEMBERS]],
                         "phi64": [m.phi.cpu().numpy() for m in m64[:SNAP_MEMBERS]],
                         "u32": m32[0].u.double().cpu().numpy(), "u64": m64[0].u.cpu().numpy()}
-    status = [m.status() for m in m32 + m64]
-    for m in m32 + m64:
+    status = [m.status() for m in m32 + m64 + m16]
+    for m in m32 + m64 + m16:
         m.close()
     return {"hist": hist, "snaps": snaps, "status": status}
 
@@ -144,13 +145,15 @@ def _check_history(ref_hist, env):
         assert lo[4] - span[4] - 0.05 <= row[6] <= hi[4] + span[4] + 0.05, (k, row[6], lo[4], hi[4])
 
 
-@pytest.mark.parametrize("dtype_name,bits", [("float32", 32), ("float64", 64)])
+@pytest.mark.parametrize("dtype_name,bits", [("float32", 32), ("float64", 64), ("float32", 16), ("float64", 16)],
+                         ids=["float32", "float64", "float32-vs-half", "float64-vs-half"])
 def test_reference_history_within_perturbation_ensemble(ensemble, dtype_name, bits):
     """sum(phi), spread extents and interface z-centre of the reference's own
     run of the whole case (2000 steps) in float32 and in float64, every 50
     steps, lie within the spread of the twelve GPU runs of the same precision
     whose initial phi differ by one float32 ulp (the spread a rounding-level
-    difference produces in this case)."""
+    difference produces in this case); and within the spread of the twelve
+    runs of the half-precision storage form."""
     ref = _ref150(dtype_name)
     assert int(ref["hist"][-1, 0]) == STEPS and len(ref["hist"]) == STEPS // 50
     _check_history(ref["hist"], ensemble["hist"][bits])
