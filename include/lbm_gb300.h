@@ -109,8 +109,8 @@ int lbm_create(const LbmParams* params, int64_t nx, int64_t ny, int64_t nz,
 /* Free the handle.  Waits for the device's queued work (as cudaFree does),
  * then returns the grid's state arrays to the process's cache of device
  * blocks, from which lbm_create takes blocks of a fitting size (at most 1/8
- * larger, same device) before it allocates; past the cache's limit they are
- * freed.  The reference frees its tensors through PyTorch's caching
+ * larger, same device) before it allocates; past the cache's limit the
+ * blocks cached longest are freed to make room.  The reference frees its tensors through PyTorch's caching
  * allocator, which keeps them likewise. */
 int lbm_destroy(LbmHandle* h);
 

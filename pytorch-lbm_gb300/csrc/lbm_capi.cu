@@ -388,12 +388,14 @@ struct CachedBlock {
   int device;
   size_t bytes;
   void* p;
+  unsigned long long seq;  // order of return to the cache (oldest evicted first)
 };
 std::mutex g_cache_mu;
 std::vector<CachedBlock> g_cache;                    // free blocks
 std::unordered_map<void*, CachedBlock> g_cache_live; // blocks handed out
 size_t g_cache_bytes = 0;
 size_t g_cache_limit = (size_t)16 << 30;
+unsigned long long g_cache_seq = 0;
 
 // Frees the cached blocks of `device` (every device for -1), each with its
 // own device current.
@@ -443,13 +445,15 @@ cudaError_t cache_alloc(void** p, size_t bytes, int device) {
   }
   if (e == cudaSuccess) {
     std::lock_guard<std::mutex> lk(g_cache_mu);
-    g_cache_live[*p] = CachedBlock{device, bytes, *p};
+    g_cache_live[*p] = CachedBlock{device, bytes, *p, 0ull};
   }
   return e;
 }
 
-// Returns a block from cache_alloc to the cache (or frees it past the
-// limit); frees anything else.  The caller has synchronised the device.
+// Returns a block from cache_alloc to the cache, first freeing the blocks
+// that have been cached longest while the limit would be exceeded (a block
+// larger than the limit is freed); frees anything else.  The caller has
+// synchronised the device.
 void cache_release(void* p) {
   if (!p) return;
   std::lock_guard<std::mutex> lk(g_cache_mu);
@@ -458,14 +462,27 @@ void cache_release(void* p) {
     cudaFree(p);
     return;
   }
-  const CachedBlock b = it->second;
+  CachedBlock b = it->second;
   g_cache_live.erase(it);
-  if (g_cache_bytes + b.bytes <= g_cache_limit) {
-    g_cache.push_back(b);
-    g_cache_bytes += b.bytes;
-  } else {
+  if (b.bytes > g_cache_limit) {
     cudaFree(p);
+    return;
   }
+  while (g_cache_bytes + b.bytes > g_cache_limit && !g_cache.empty()) {
+    size_t old = 0;
+    for (size_t i = 1; i < g_cache.size(); ++i)
+      if (g_cache[i].seq < g_cache[old].seq) old = i;
+    int cur = -1;
+    (void)cudaGetDevice(&cur);
+    if (cudaSetDevice(g_cache[old].device) == cudaSuccess) cudaFree(g_cache[old].p);
+    if (cur >= 0) (void)cudaSetDevice(cur);
+    g_cache_bytes -= g_cache[old].bytes;
+    g_cache[old] = g_cache.back();
+    g_cache.pop_back();
+  }
+  b.seq = ++g_cache_seq;
+  g_cache.push_back(b);
+  g_cache_bytes += b.bytes;
 }
 
 void free_all(LbmHandle* h) {

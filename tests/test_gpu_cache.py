@@ -142,3 +142,28 @@ def test_host_inputs_read_in_place_equal_staged_copy(tmp_path):
         res.append([d[k] for k in sorted(d.files)])
     for a, b in zip(*res):
         assert a.tobytes() == b.tobytes()
+
+
+def test_cache_stays_within_its_limit():
+    """Past the limit the blocks cached longest make room for the ones just
+    returned, and a block larger than the limit is freed: the cache never
+    holds more than its limit, whatever the order of grids."""
+    from lbm import _native as nat
+    from lbm.batch import footprint
+    nat.cache_trim()
+    try:
+        nat.cache_limit(1 << 20)  # below one population array of either grid
+        for name in ("ridge_l162", "cfg1_flat64", "ridge_l162"):
+            _solver(name, torch.float32).close()
+            assert 0 < nat.cache_bytes() <= 1 << 20
+        small = footprint(CASES["ridge_l162"]["grid"], torch.float32)
+        limit = int(1.5 * small)
+        nat.cache_limit(limit)
+        for name in ("ridge_l162", "cfg1_flat64", "ridge_l162", "cfg1_flat64"):
+            s = _solver(name, torch.float32)
+            assert nat.cache_bytes() <= limit
+            s.close()
+            assert 0 < nat.cache_bytes() <= limit
+    finally:
+        nat.cache_limit(16 << 30)
+        nat.cache_trim()
